@@ -1,0 +1,153 @@
+/*
+ * nmgpu.h -- C-ABI of the GB300 (sm_103a) eigensolver for planetary normal
+ * modes: the drop-in for the operator callbacks and the eigensolve driver of
+ * js1019/NormalModes.
+ *
+ * The reference hands pEVSL three callbacks with the Fortran signature
+ * (v, w, mymv) -- v, w real*8(n_loc) by reference, mymv the opaque
+ * `type(mvparameters)` context (src/mod_cg_datatype.f90:88-115):
+ *
+ *   sparseAV   src/mod_matvec.f90:445-458   w = D A D v            (solid only)
+ *   sparsefsAV src/mod_matvec.f90:498-520   w = D(Ad D v + E D_p Cheb_Ap(D_p ET D v))
+ *   sparseBV   src/mod_matvec.f90:461-472   w = B_s v
+ *   solveBV    src/mod_matvec.f90:475-483   w = Cheb_B(v)   (pEVSL chebiter type 2)
+ *
+ * registered at src/mod_pevsl.f90:69-80, and runs the whole solve in
+ * `pnm_apply_pevsl` (src/mod_pevsl.f90:16-222).  Here one opaque nm_ctx owns
+ * the operators on one GPU; nm_amv / nm_bmv / nm_bsolve are the callbacks
+ * (host vectors, or device vectors with the *_dev variants) and nm_solve is
+ * the whole filtered-Lanczos solve, so the Krylov basis never leaves the GPU.
+ *
+ * Conventions: 0-based int32 CSR (`col - 1` of src/mod_matvec.f90:59), float64
+ * values, the caller keeps ownership of every array it passes (the library
+ * copies), every entry point returns an NM_* status, nm_last_error() explains
+ * the last failure of a context.  Calls on one context are not thread-safe;
+ * distinct contexts are independent.  There is no CPU fallback: without a
+ * usable GPU nm_create fails with NM_ERR_CUDA.
+ */
+#ifndef NMGPU_H
+#define NMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NM_OK 0
+#define NM_ERR_ARG (-1)     /* bad argument / inconsistent sizes            */
+#define NM_ERR_CUDA (-2)    /* CUDA runtime error or no usable device        */
+#define NM_ERR_OOM (-3)     /* device allocation failed                      */
+#define NM_ERR_NOCONV (-4)  /* Lanczos hit MAXIT before the trace converged  */
+#define NM_ERR_TIMEOUT (-5) /* a bounded device-side wait gave up            */
+#define NM_ERR_NUMERIC (-6) /* non-positive diagonal, NaN/Inf, breakdown     */
+
+/* One CSR matrix, 0-based. */
+typedef struct {
+  int nrows, ncols;
+  const int* rowptr; /* nrows + 1 */
+  const int* col;    /* rowptr[nrows] */
+  const double* val; /* rowptr[nrows] */
+} nm_csr;
+
+typedef struct {
+  int porder;        /* pOrder of global_conf: 1 or 2 (selects Chebyshev degrees) */
+  int device;        /* CUDA device ordinal                                      */
+  int b_cheb_deg;    /* 0: 45 (P2) / 25 (P1), src/mod_matvec.f90:88-92           */
+  int ap_cheb_deg;   /* 0: max(min(int(cond),15)*3,100) (P2) / 25 (P1), :167-171  */
+  double b_bounds[2];  /* if b_bounds[1] > 0: use instead of Lanczos bounds of B_s */
+  double ap_bounds[2]; /* idem for Ap_s                                           */
+  int precision;     /* NM_PREC_FP64 or NM_PREC_MIXED (FP32 filter SpMVs)        */
+  int verbose;       /* print the reference's progress lines                      */
+} nm_opts;
+
+#define NM_PREC_FP64 0
+#define NM_PREC_MIXED 1
+
+typedef struct {
+  int maxit;          /* 0: 3*max(4*802,2000) = 9624 (src/mod_pevsl.f90:116-119) */
+  double tol;         /* 0: 1e-5 (src/mod_pevsl.f90:52)                            */
+  double thresh_int;  /* 0: 0.8 (src/mod_pevsl.f90:108)                            */
+  double thresh_ext;  /* 0: 0.7 (src/mod_pevsl.f90:109)                            */
+  int mlan_bounds;    /* 0: 3000 (src/mod_pevsl.f90:49)                            */
+  double ab_bounds[2];/* if ab_bounds[1] > 0: skip LANBOUNDS(B^-1 A), use these    */
+  int damping;        /* 0/1: Jackson, 2: Lanczos sigma                            */
+  int want_vectors;   /* copy eigenvectors to the result                           */
+  int unscale;        /* vectors as x = y .* D (src/mod_pevsl.f90:199) not y       */
+  int use_graph;      /* capture the filter in a CUDA graph (default on)           */
+} nm_solve_opts;
+
+typedef struct {
+  int nev;            /* eigenpairs found in [a, b]                                */
+  int n;              /* vector length                                              */
+  double* lam;        /* nev, ascending                                             */
+  double* vec;        /* n * nev column-major (if want_vectors), else NULL          */
+  double* err_ref;    /* sqrt(sum (Ay - lam By)^2 / N) / |lam|, src/mod_pevsl.f90:158 */
+  double* res2;       /* ||Ay - lam By||_2 / |lam| with ||y||_B = 1                  */
+  double xintv[4];    /* [a, b, lmin, lmax] of src/mod_pevsl.f90:93-103              */
+  int pol_deg;        /* filter degree                                               */
+  double pol_gam, pol_bar;
+  int lanczos_steps;
+  int nritz_above_bar;
+  double t_bounds, t_filter_design, t_lanczos, t_ritz, t_total; /* seconds        */
+  long long n_amv, n_bsolve, n_spmv; /* operator applications / SpMV launches       */
+} nm_result;
+
+typedef struct nm_ctx nm_ctx;
+
+/* Operator construction: replaces setupmatvec (src/mod_matvec.f90:24-250).
+ * Solid-only model: A = stiffness, Ap = E = ET = NULL.  Fluid-solid model:
+ * A = Ad, plus Ap (reference sign, negative definite), E, ET.  The library
+ * computes D = diag(B)^-1/2, D_p = diag(-Ap)^-1/2, the scaled operators, the
+ * Lanczos bounds of B_s and Ap_s and the Chebyshev set-ups itself. */
+int nm_create(nm_ctx** out, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, const nm_csr* E,
+              const nm_csr* ET, const nm_opts* opts);
+void nm_destroy(nm_ctx* ctx);
+void nm_default_opts(nm_opts* o);
+void nm_default_solve_opts(nm_solve_opts* o);
+
+/* Callbacks, host vectors of length n (copies in and out). */
+int nm_amv(nm_ctx* ctx, const double* x, double* y);    /* sparseAV / sparsefsAV */
+int nm_bmv(nm_ctx* ctx, const double* x, double* y);    /* sparseBV              */
+int nm_bsolve(nm_ctx* ctx, const double* x, double* y); /* solveBV               */
+/* Same on device pointers, enqueued on the context's stream (no sync). */
+int nm_amv_dev(nm_ctx* ctx, const double* x, double* y);
+int nm_bmv_dev(nm_ctx* ctx, const double* x, double* y);
+int nm_bsolve_dev(nm_ctx* ctx, const double* x, double* y);
+/* Blocks of ncols column vectors with leading dimension ld (host memory). */
+int nm_amv_block(nm_ctx* ctx, const double* X, double* Y, int ncols, int ld);
+int nm_bmv_block(nm_ctx* ctx, const double* X, double* Y, int ncols, int ld);
+int nm_bsolve_block(nm_ctx* ctx, const double* X, double* Y, int ncols, int ld);
+
+/* The whole solve of pnm_apply_pevsl for [f_lo, f_hi] mHz. */
+int nm_solve(nm_ctx* ctx, double f_lo_mhz, double f_hi_mhz, const nm_solve_opts* opts, nm_result* res);
+void nm_result_free(nm_result* res);
+
+/* Introspection. */
+typedef struct {
+  int n, np, fs, porder, precision;
+  long long nnz_a, nnz_b, nnz_ap, nnz_e, nnz_et;
+  double b_bounds[2], ap_bounds[2];
+  int b_cheb_deg, ap_cheb_deg;
+  double t_setup;        /* seconds spent in nm_create                        */
+  long long h2d_bytes;   /* bytes copied host -> device by nm_create          */
+  size_t device_bytes;   /* device memory held by the context                 */
+} nm_info;
+int nm_get_info(nm_ctx* ctx, nm_info* info);
+void* nm_get_stream(nm_ctx* ctx); /* cudaStream_t of the context */
+const char* nm_last_error(nm_ctx* ctx);
+int nm_sync(nm_ctx* ctx);
+
+/* Kernel-level timing of the dominant operators (CUDA events on the
+ * context's stream), for roofline reporting: runs `reps` back-to-back
+ * applications of the selected operator on device vectors and returns the
+ * mean time per application in milliseconds and the algorithmic bytes one
+ * application moves.  which: 0 = A-op, 1 = B SpMV, 2 = B Chebyshev solve,
+ * 3 = one filter degree step (B-solve + A-op + recurrence). */
+int nm_time_op(nm_ctx* ctx, int which, int reps, double* ms_per_op, double* bytes_per_op, int* launches_per_op);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,303 @@
+"""Python host binding of ``libnmgpu.so`` (ctypes over the C-ABI of
+``include/nmgpu.h``).
+
+:class:`Solver` mirrors the reference's solve driver: construction is
+``setupmatvec`` (src/mod_matvec.f90:24-250), :meth:`Solver.amv`,
+:meth:`Solver.bmv`, :meth:`Solver.bsolve` are the callbacks
+``sparseAV``/``sparsefsAV``, ``sparseBV``, ``solveBV`` (src/mod_matvec.f90:445-520)
+and :meth:`Solver.solve` is ``pnm_apply_pevsl`` (src/mod_pevsl.f90:16-222).
+
+There is no CPU fallback: if the CUDA library cannot be loaded or no GPU is
+usable, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+
+NM_PREC_FP64 = 0
+NM_PREC_MIXED = 1
+
+ERRORS = {0: "NM_OK", -1: "NM_ERR_ARG", -2: "NM_ERR_CUDA", -3: "NM_ERR_OOM", -4: "NM_ERR_NOCONV",
+          -5: "NM_ERR_TIMEOUT", -6: "NM_ERR_NUMERIC"}
+
+EXPORTS = [
+    "nm_create", "nm_destroy", "nm_default_opts", "nm_default_solve_opts", "nm_amv", "nm_bmv", "nm_bsolve",
+    "nm_amv_dev", "nm_bmv_dev", "nm_bsolve_dev", "nm_amv_block", "nm_bmv_block", "nm_bsolve_block", "nm_solve",
+    "nm_result_free", "nm_get_info", "nm_get_stream", "nm_last_error", "nm_sync", "nm_time_op",
+]
+
+
+class NmCsr(C.Structure):
+    _fields_ = [("nrows", C.c_int), ("ncols", C.c_int), ("rowptr", C.POINTER(C.c_int)),
+                ("col", C.POINTER(C.c_int)), ("val", C.POINTER(C.c_double))]
+
+
+class NmOpts(C.Structure):
+    _fields_ = [("porder", C.c_int), ("device", C.c_int), ("b_cheb_deg", C.c_int), ("ap_cheb_deg", C.c_int),
+                ("b_bounds", C.c_double * 2), ("ap_bounds", C.c_double * 2), ("precision", C.c_int),
+                ("verbose", C.c_int)]
+
+
+class NmSolveOpts(C.Structure):
+    _fields_ = [("maxit", C.c_int), ("tol", C.c_double), ("thresh_int", C.c_double), ("thresh_ext", C.c_double),
+                ("mlan_bounds", C.c_int), ("ab_bounds", C.c_double * 2), ("damping", C.c_int),
+                ("want_vectors", C.c_int), ("unscale", C.c_int), ("use_graph", C.c_int)]
+
+
+class NmResult(C.Structure):
+    _fields_ = [("nev", C.c_int), ("n", C.c_int), ("lam", C.POINTER(C.c_double)), ("vec", C.POINTER(C.c_double)),
+                ("err_ref", C.POINTER(C.c_double)), ("res2", C.POINTER(C.c_double)), ("xintv", C.c_double * 4),
+                ("pol_deg", C.c_int), ("pol_gam", C.c_double), ("pol_bar", C.c_double),
+                ("lanczos_steps", C.c_int), ("nritz_above_bar", C.c_int),
+                ("t_bounds", C.c_double), ("t_filter_design", C.c_double), ("t_lanczos", C.c_double),
+                ("t_ritz", C.c_double), ("t_total", C.c_double),
+                ("n_amv", C.c_longlong), ("n_bsolve", C.c_longlong), ("n_spmv", C.c_longlong)]
+
+
+class NmInfo(C.Structure):
+    _fields_ = [("n", C.c_int), ("np", C.c_int), ("fs", C.c_int), ("porder", C.c_int), ("precision", C.c_int),
+                ("nnz_a", C.c_longlong), ("nnz_b", C.c_longlong), ("nnz_ap", C.c_longlong),
+                ("nnz_e", C.c_longlong), ("nnz_et", C.c_longlong), ("b_bounds", C.c_double * 2),
+                ("ap_bounds", C.c_double * 2), ("b_cheb_deg", C.c_int), ("ap_cheb_deg", C.c_int),
+                ("t_setup", C.c_double), ("h2d_bytes", C.c_longlong), ("device_bytes", C.c_size_t)]
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return os.path.join(_build.LIBDIR, "libnmgpu.so")
+
+
+def lib() -> C.CDLL:
+    """Load libnmgpu.so (building it if this is a fresh tree)."""
+    global _lib
+    if _lib is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            path = _build.build_gpu()
+        L = C.CDLL(path)
+        vp, dp = C.c_void_p, C.POINTER(C.c_double)
+        L.nm_create.argtypes = [C.POINTER(vp)] + [C.POINTER(NmCsr)] * 5 + [C.POINTER(NmOpts)]
+        L.nm_destroy.argtypes = [vp]
+        L.nm_default_opts.argtypes = [C.POINTER(NmOpts)]
+        L.nm_default_solve_opts.argtypes = [C.POINTER(NmSolveOpts)]
+        for f in ("nm_amv", "nm_bmv", "nm_bsolve", "nm_amv_dev", "nm_bmv_dev", "nm_bsolve_dev"):
+            getattr(L, f).argtypes = [vp, C.c_void_p, C.c_void_p]
+        for f in ("nm_amv_block", "nm_bmv_block", "nm_bsolve_block"):
+            getattr(L, f).argtypes = [vp, dp, dp, C.c_int, C.c_int]
+        L.nm_solve.argtypes = [vp, C.c_double, C.c_double, C.POINTER(NmSolveOpts), C.POINTER(NmResult)]
+        L.nm_result_free.argtypes = [C.POINTER(NmResult)]
+        L.nm_get_info.argtypes = [vp, C.POINTER(NmInfo)]
+        L.nm_get_stream.argtypes = [vp]
+        L.nm_get_stream.restype = C.c_void_p
+        L.nm_last_error.argtypes = [vp]
+        L.nm_last_error.restype = C.c_char_p
+        L.nm_sync.argtypes = [vp]
+        L.nm_time_op.argtypes = [vp, C.c_int, C.c_int, dp, dp, C.POINTER(C.c_int)]
+        L.nm_test_find_pol.argtypes = [dp, C.c_double, C.c_double, C.c_int, dp, C.c_int, dp]
+        L.nm_test_tridiag.argtypes = [dp, dp, C.c_int, C.c_double, C.c_double, dp, dp, C.c_int]
+        L.nm_test_sell.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), dp,
+                                   C.POINTER(C.c_int), C.POINTER(C.c_longlong)]
+        L.nm_test_sell.restype = C.c_longlong
+        L.nm_test_start_vector.argtypes = [C.c_int, dp]
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class NmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+@dataclass
+class SolveResult:
+    lam: np.ndarray
+    vec: np.ndarray | None
+    err_ref: np.ndarray
+    res2: np.ndarray
+    xintv: tuple
+    pol_deg: int
+    pol_gam: float
+    pol_bar: float
+    lanczos_steps: int
+    nritz_above_bar: int
+    times: dict
+    counts: dict
+
+
+class Solver:
+    """Operators of one model on one GPU and the filtered-Lanczos solve."""
+
+    def __init__(self, mats: dict, porder: int, device: int = 0, precision: int = NM_PREC_FP64,
+                 b_bounds=None, ap_bounds=None, b_cheb_deg: int = 0, ap_cheb_deg: int = 0, verbose: bool = False):
+        L = lib()
+        self.fs = "Ad" in mats
+        self._keep = []
+
+        def csr(m):
+            rp = np.ascontiguousarray(m.rowptr, dtype=np.int32)
+            ci = np.ascontiguousarray(m.col, dtype=np.int32)
+            v = np.ascontiguousarray(m.val, dtype=np.float64)
+            self._keep += [rp, ci, v]
+            return NmCsr(m.shape[0], m.shape[1], rp.ctypes.data_as(C.POINTER(C.c_int)),
+                         ci.ctypes.data_as(C.POINTER(C.c_int)), _dp(v))
+
+        A = csr(mats["Ad"] if self.fs else mats["A"])
+        B = csr(mats["B"])
+        Ap = csr(mats["Ap"]) if self.fs else None
+        E = csr(mats["E"]) if self.fs else None
+        ET = csr(mats["ET"]) if self.fs else None
+        o = NmOpts()
+        L.nm_default_opts(C.byref(o))
+        o.porder = porder
+        o.device = device
+        o.precision = precision
+        o.verbose = int(verbose)
+        o.b_cheb_deg = b_cheb_deg
+        o.ap_cheb_deg = ap_cheb_deg
+        if b_bounds is not None:
+            o.b_bounds[0], o.b_bounds[1] = b_bounds
+        if ap_bounds is not None:
+            o.ap_bounds[0], o.ap_bounds[1] = ap_bounds
+        h = C.c_void_p()
+        ref = lambda x: C.byref(x) if x is not None else None
+        rc = L.nm_create(C.byref(h), ref(A), ref(B), ref(Ap), ref(E), ref(ET), C.byref(o))
+        self._h = h
+        if rc != 0:
+            msg = L.nm_last_error(h).decode() if h else "nm_create failed"
+            L.nm_destroy(h)
+            self._h = C.c_void_p()
+            raise NmError(rc, msg)
+        self._keep = []  # the library copied the arrays
+        self.n = mats["B"].shape[0]
+
+    # -- callbacks (host vectors)
+    def _call(self, fn, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty_like(x)
+        rc = getattr(lib(), fn)(self._h, x.ctypes.data, y.ctypes.data)
+        self._check(rc)
+        return y
+
+    def _check(self, rc):
+        if rc != 0:
+            raise NmError(rc, lib().nm_last_error(self._h).decode())
+
+    def amv(self, x):
+        return self._call("nm_amv", x)
+
+    def bmv(self, x):
+        return self._call("nm_bmv", x)
+
+    def bsolve(self, x):
+        return self._call("nm_bsolve", x)
+
+    def block(self, which: str, X: np.ndarray) -> np.ndarray:
+        X = np.asfortranarray(X, dtype=np.float64)
+        Y = np.empty_like(X)
+        fn = {"amv": "nm_amv_block", "bmv": "nm_bmv_block", "bsolve": "nm_bsolve_block"}[which]
+        self._check(getattr(lib(), fn)(self._h, _dp(X), _dp(Y), X.shape[1], X.shape[0]))
+        return Y
+
+    def info(self) -> NmInfo:
+        i = NmInfo()
+        self._check(lib().nm_get_info(self._h, C.byref(i)))
+        return i
+
+    @property
+    def stream(self) -> int:
+        return lib().nm_get_stream(self._h)
+
+    def time_op(self, which: int, reps: int = 20):
+        ms, by, la = C.c_double(), C.c_double(), C.c_int()
+        self._check(lib().nm_time_op(self._h, which, reps, C.byref(ms), C.byref(by), C.byref(la)))
+        return ms.value, by.value, la.value
+
+    def solve(self, lowfreq: float, upfreq: float, maxit: int = 0, tol: float = 0.0, ab_bounds=None,
+              want_vectors: bool = True, unscale: bool = False, use_graph: bool = True, damping: int = 1,
+              mlan_bounds: int = 0, allow_noconv: bool = False) -> SolveResult:
+        L = lib()
+        o = NmSolveOpts()
+        L.nm_default_solve_opts(C.byref(o))
+        o.maxit = maxit
+        o.tol = tol
+        o.want_vectors = int(want_vectors)
+        o.unscale = int(unscale)
+        o.use_graph = int(use_graph)
+        o.damping = damping
+        o.mlan_bounds = mlan_bounds
+        if ab_bounds is not None:
+            o.ab_bounds[0], o.ab_bounds[1] = ab_bounds
+        r = NmResult()
+        rc = L.nm_solve(self._h, lowfreq, upfreq, C.byref(o), C.byref(r))
+        if rc != 0 and not (allow_noconv and rc == -4):
+            L.nm_result_free(C.byref(r))
+            self._check(rc)
+        try:
+            nev, n = r.nev, r.n
+            arr = lambda p: np.ctypeslib.as_array(p, shape=(max(nev, 1),))[:nev].copy() if nev else np.zeros(0)
+            vec = None
+            if want_vectors and nev:
+                vec = np.ctypeslib.as_array(r.vec, shape=(nev * n,)).reshape(nev, n).T.copy()
+            return SolveResult(arr(r.lam), vec, arr(r.err_ref), arr(r.res2), tuple(r.xintv), r.pol_deg, r.pol_gam,
+                               r.pol_bar, r.lanczos_steps, r.nritz_above_bar,
+                               {"bounds": r.t_bounds, "filter_design": r.t_filter_design, "lanczos": r.t_lanczos,
+                                "ritz": r.t_ritz, "total": r.t_total},
+                               {"amv": r.n_amv, "bsolve": r.n_bsolve, "spmv": r.n_spmv})
+        finally:
+            L.nm_result_free(C.byref(r))
+
+    def close(self):
+        if self._h:
+            lib().nm_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# -- host-only helpers (no GPU needed)
+def find_pol(xintv, thresh_int=0.8, thresh_ext=0.7, damping=1, max_deg=10000):
+    mu = np.zeros(max_deg + 1)
+    out = np.zeros(4)
+    x = np.ascontiguousarray(xintv, dtype=np.float64)
+    deg = lib().nm_test_find_pol(_dp(x), thresh_int, thresh_ext, damping, _dp(mu), max_deg, _dp(out))
+    return deg, mu[: deg + 1].copy(), tuple(out)
+
+
+def tridiag_eig(d, e, lo, hi, cap=None):
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    e = np.ascontiguousarray(e, dtype=np.float64)
+    k = len(d)
+    cap = cap or k
+    lam = np.zeros(cap)
+    vec = np.zeros(cap * k)
+    m = lib().nm_test_tridiag(_dp(d), _dp(e if len(e) else np.zeros(1)), k, lo, hi, _dp(lam), _dp(vec), cap)
+    return lam[:m].copy(), vec[: m * k].reshape(m, k).T.copy()
+
+
+def start_vector(n: int) -> np.ndarray:
+    out = np.zeros(n)
+    lib().nm_test_start_vector(n, _dp(out))
+    return out
