@@ -82,11 +82,12 @@ int alloc_work(nm_ctx* c) {
       c->dev_bytes += s32[i] * sizeof(float);
     }
   }
-  c->red_cap = 1 << 20;
+  c->red_cap = kMaxCols * kRedParts;
   NM_CUDA(c, cudaMalloc(&c->red, (size_t)c->red_cap * sizeof(double)));
+  NM_CUDA(c, cudaMalloc(&c->hbuf, (size_t)kMaxCols * sizeof(double)));
   NM_CUDA(c, cudaMalloc(&c->scal, 64 * sizeof(double)));
   NM_CUDA(c, cudaMallocHost(&c->h_scal, 64 * sizeof(double)));
-  c->dev_bytes += (size_t)c->red_cap * 8 + 512;
+  c->dev_bytes += (size_t)c->red_cap * 8 + (size_t)kMaxCols * 8 + 512;
   return NM_OK;
 }
 
@@ -226,6 +227,7 @@ void nm_destroy(nm_ctx* c) {
   cudaFree(c->D);
   cudaFree(c->Dp);
   cudaFree(c->red);
+  cudaFree(c->hbuf);
   cudaFree(c->scal);
   if (c->h_scal) cudaFreeHost(c->h_scal);
   if (c->stream) cudaStreamDestroy(c->stream);

@@ -87,11 +87,13 @@ struct nm_ctx {
   // work vectors (device)
   double* w[16] = {nullptr};
   float* w32[12] = {nullptr};
-  double* red = nullptr;   // reduction scratch
-  double* scal = nullptr;  // device scalars
+  double* red = nullptr;   // reduction scratch (kMaxCols * kRedParts doubles)
+  double* hbuf = nullptr;  // Gram-Schmidt coefficients (kMaxCols doubles)
+  double* scal = nullptr;  // device scalars (64 doubles)
   double* h_scal = nullptr;  // pinned host scalars
   int red_cap = 0;
   std::string err;
+  bool cuda_failed = false;
   double t_setup = 0;
   long long h2d_bytes = 0;
   size_t dev_bytes = 0;
@@ -172,6 +174,7 @@ void dev_dot(const double* x, const double* y, int n, double* red, double* out, 
 void dev_sqrt_inplace(double* x, cudaStream_t s);
 // reorth: h = V(:, 0..k)^T z ; z -= Z(:, 0..k) h     (red >= ncol * kRedParts)
 constexpr int kRedParts = 64;
+constexpr int kMaxCols = 16384;  // largest Krylov basis (MAXIT = 9624 in the reference)
 void reorth_pass(const Basis& V, const Basis& Z, int ncol, double* z, int n, double* red, double* h, cudaStream_t s);
 
 }  // namespace nmg

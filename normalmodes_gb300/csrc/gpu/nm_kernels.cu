@@ -406,6 +406,9 @@ void dev_dot(const double* x, const double* y, int n, double* red, double* out, 
 void dev_sqrt_inplace(double* x, cudaStream_t s) { k_sqrt<<<1, 32, 0, s>>>(x); }
 
 void reorth_pass(const Basis& V, const Basis& Z, int ncol, double* z, int n, double* red, double* h, cudaStream_t s) {
+  // red holds ncol * kRedParts partial sums and h ncol coefficients; both are
+  // sized for kMaxCols columns by the context.
+  if (ncol > kMaxCols) return;
   dim3 g((ncol + kTC - 1) / kTC, kRedParts);
   k_gs_dot<<<g, kThreads, 0, s>>>(V.d_chunks, V.ld, ncol, z, n, red);
   k_gs_sum<<<nblk(ncol), kThreads, 0, s>>>(red, ncol, h);

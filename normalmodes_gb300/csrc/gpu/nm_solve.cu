@@ -73,10 +73,18 @@ __global__ void k_resid(const double* __restrict__ w, const double* __restrict__
   if (i < n) r[i] = fma(-th, bw[i], w[i]);
 }
 
+// Dot product brought back to the host.  A CUDA failure is recorded in the
+// context (c->cuda_failed) and returns NaN, which every caller treats as an
+// error.
 double dot_sync(nm_ctx* c, const double* x, const double* y, int n) {
   dev_dot(x, y, n, c->red, c->scal, c->stream);
-  cudaMemcpyAsync(c->h_scal, c->scal, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
-  cudaStreamSynchronize(c->stream);
+  cudaError_t e = cudaMemcpyAsync(c->h_scal, c->scal, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    c->cuda_failed = true;
+    set_err(c, NM_ERR_CUDA, std::string("device error: ") + cudaGetErrorString(e));
+    return std::nan("");
+  }
   return c->h_scal[0];
 }
 
@@ -103,7 +111,7 @@ using Apply = std::function<void(const double*, double*)>;
 // product, z = B~ v carried) otherwise.
 int lanczos_bounds(nm_ctx* c, int nn, const Apply& op, const Apply& solve, int msteps, double tol, double* lmin,
                    double* lmax, int* steps, double* znew, double* vnew) {
-  msteps = std::min(msteps, nn);
+  msteps = std::min(std::min(msteps, nn), kMaxCols - 1);
   const bool gen = (bool)solve;
   Basis V, Zb;
   int rc;
@@ -134,7 +142,7 @@ int lanczos_bounds(nm_ctx* c, int nn, const Apply& op, const Apply& solve, int m
     const double a = dot_sync(c, V.col(k), znew, nn);
     alpha.push_back(a);
     dev_axpy(znew, Z.col(k), -a, nn, c->stream);
-    for (int p = 0; p < 2; ++p) reorth_pass(V, Z, k + 1, znew, nn, c->red, c->scal + 8, c->stream);
+    for (int p = 0; p < 2; ++p) reorth_pass(V, Z, k + 1, znew, nn, c->red, c->hbuf, c->stream);
     double b;
     if (gen) {
       solve(znew, vnew);
@@ -145,7 +153,7 @@ int lanczos_bounds(nm_ctx* c, int nn, const Apply& op, const Apply& solve, int m
     if (!std::isfinite(a) || !std::isfinite(b)) {
       free_basis(V);
       free_basis(Zb);
-      return set_err(c, NM_ERR_NUMERIC, "non-finite value in Lanczos bounds");
+      return c->cuda_failed ? NM_ERR_CUDA : set_err(c, NM_ERR_NUMERIC, "non-finite value in Lanczos bounds");
     }
     beta.push_back(b);
     const bool last = (k == msteps - 1) || b == 0.0;
@@ -338,7 +346,8 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
   else nm_default_solve_opts(&o);
   const int n = c->n;
   const int maxit_def = 3 * std::max(4 * 802, 2000);
-  int maxit = std::min(o.maxit > 0 ? o.maxit : maxit_def, n);
+  int maxit = std::min(std::min(o.maxit > 0 ? o.maxit : maxit_def, n), kMaxCols - 1);
+  c->cuda_failed = false;
   const double tol = o.tol > 0 ? o.tol : 1e-5;
   const double thr_int = o.thresh_int > 0 ? o.thresh_int : 0.8;
   const double thr_ext = o.thresh_ext > 0 ? o.thresh_ext : 0.7;
@@ -381,6 +390,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
     NM_CUDA(c, cudaMemcpyAsync(Z.col(0), h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     bsolve64(c, Z.col(0), V.col(0));
     const double t = 1.0 / std::sqrt(dot_sync(c, V.col(0), Z.col(0), n));
+    if (!std::isfinite(t)) return c->cuda_failed ? NM_ERR_CUDA : set_err(c, NM_ERR_NUMERIC, "B-norm of start vector");
     dev_scale(Z.col(0), Z.col(0), t, n, c->stream);
     dev_scale(V.col(0), V.col(0), t, n, c->stream);
   }
@@ -419,13 +429,13 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
     const double alpha = dot_sync(c, V.col(k), znew, n);
     dT.push_back(alpha);
     dev_axpy(znew, Z.col(k), -alpha, n, c->stream);
-    for (int p = 0; p < 2; ++p) reorth_pass(V, Z, k + 1, znew, n, c->red, c->scal + 8, c->stream);
+    for (int p = 0; p < 2; ++p) reorth_pass(V, Z, k + 1, znew, n, c->red, c->hbuf, c->stream);
     double* vnew = c->w[1];
     bsolve64(c, znew, vnew);
     beta = std::sqrt(std::max(dot_sync(c, vnew, znew, n), 0.0));
     if (!std::isfinite(alpha) || !std::isfinite(beta)) {
       if (gexec) cudaGraphExecDestroy(gexec);
-      return set_err(c, NM_ERR_NUMERIC, "non-finite Lanczos coefficient");
+      return c->cuda_failed ? NM_ERR_CUDA : set_err(c, NM_ERR_NUMERIC, "non-finite Lanczos coefficient");
     }
     kdim = k + 1;
     if (beta == 0.0) {
