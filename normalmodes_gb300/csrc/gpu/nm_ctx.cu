@@ -86,8 +86,35 @@ int alloc_work(nm_ctx* c) {
   NM_CUDA(c, cudaMalloc(&c->red, (size_t)c->red_cap * sizeof(double)));
   NM_CUDA(c, cudaMalloc(&c->hbuf, (size_t)kMaxCols * sizeof(double)));
   NM_CUDA(c, cudaMalloc(&c->scal, 64 * sizeof(double)));
+  NM_CUDA(c, cudaMalloc(&c->bar, sizeof(GridBar)));
+  NM_CUDA(c, cudaMalloc(&c->d_status, sizeof(int)));
+  NM_CUDA(c, cudaMemset(c->bar, 0, sizeof(GridBar)));
+  NM_CUDA(c, cudaMemset(c->d_status, 0, sizeof(int)));
+  c->coop_blocks = coop_blocks_for_persistent();
   NM_CUDA(c, cudaMallocHost(&c->h_scal, 64 * sizeof(double)));
   c->dev_bytes += (size_t)c->red_cap * 8 + (size_t)kMaxCols * 8 + 512;
+  return NM_OK;
+}
+
+int upload_cheb(nm_ctx* c, ChebSetup& ch) {
+  cudaFree(ch.d_coef);
+  ch.d_coef = nullptr;
+  std::vector<double> buf(ch.a);
+  buf.insert(buf.end(), ch.c.begin(), ch.c.end());
+  if (buf.empty()) return NM_OK;
+  NM_CUDA(c, cudaMalloc(&ch.d_coef, sizeof(double) * buf.size()));
+  NM_CUDA(c, cudaMemcpy(ch.d_coef, buf.data(), sizeof(double) * buf.size(), cudaMemcpyHostToDevice));
+  return NM_OK;
+}
+
+int check_status(nm_ctx* c) {
+  int st = 0;
+  NM_CUDA(c, cudaMemcpyAsync(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  NM_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (st != 0) {
+    c->cuda_failed = true;
+    return set_err(c, NM_ERR_TIMEOUT, "a grid barrier of the persistent Chebyshev kernel timed out");
+  }
   return NM_OK;
 }
 
@@ -193,6 +220,7 @@ int nm_create(nm_ctx** out, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, 
     if (c->verbose) printf(" B cond. number %g %g %g\n", c->chebB.lmax / c->chebB.lmin, c->chebB.lmin, c->chebB.lmax);
   }
   cheb_coefs(c->chebB);
+  if ((rc = upload_cheb(c, c->chebB))) return bail(rc);
   if (c->fs) {
     if (o.ap_bounds[1] > 0) {
       c->chebAp.lmin = o.ap_bounds[0];
@@ -207,6 +235,7 @@ int nm_create(nm_ctx** out, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, 
     else if (c->porder == 2) c->chebAp.deg = std::max(std::min((int)(c->chebAp.lmax / c->chebAp.lmin), 15) * 3, 100);
     else c->chebAp.deg = 25;
     cheb_coefs(c->chebAp);
+    if ((rc = upload_cheb(c, c->chebAp))) return bail(rc);
   }
   NM_CUDA(c, cudaStreamSynchronize(c->stream));
   c->t_setup = now_s() - t0;
@@ -229,6 +258,10 @@ void nm_destroy(nm_ctx* c) {
   cudaFree(c->red);
   cudaFree(c->hbuf);
   cudaFree(c->scal);
+  cudaFree(c->bar);
+  cudaFree(c->d_status);
+  cudaFree(c->chebB.d_coef);
+  cudaFree(c->chebAp.d_coef);
   if (c->h_scal) cudaFreeHost(c->h_scal);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -296,7 +329,7 @@ static int host_call(nm_ctx* c, int which, const double* X, double* Y, int ncols
   }
   NM_CUDA(c, cudaStreamSynchronize(c->stream));
   NM_CUDA(c, cudaGetLastError());
-  return NM_OK;
+  return check_status(c);
 }
 
 int nm_amv(nm_ctx* c, const double* x, double* y) { return host_call(c, 0, x, y, 1, c ? c->n : 0); }

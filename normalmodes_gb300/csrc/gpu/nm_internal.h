@@ -59,7 +59,15 @@ struct ChebSetup {
   int deg = 0;
   std::vector<double> a, c;  // per-iteration recurrence coefficients
   double inv_theta = 0;
+  double* d_coef = nullptr;  // device copy: a[0..deg-1], c[0..deg-1]
 };
+
+// State of the bounded software grid barrier of the persistent kernels.
+struct GridBar {
+  unsigned int count;
+  unsigned int gen;
+};
+constexpr long long kSpinLimit = 1ll << 24;  // polls (~1 s) before a barrier wait gives up
 
 // Basis of Lanczos vectors, allocated in chunks of kChunk columns.
 struct Basis {
@@ -90,7 +98,10 @@ struct nm_ctx {
   double* red = nullptr;   // reduction scratch (kMaxCols * kRedParts doubles)
   double* hbuf = nullptr;  // Gram-Schmidt coefficients (kMaxCols doubles)
   double* scal = nullptr;  // device scalars (64 doubles)
-  double* h_scal = nullptr;  // pinned host scalars
+  nmg::GridBar* bar = nullptr;  // grid barrier of the persistent Chebyshev kernel
+  int* d_status = nullptr;      // sticky device error word (1 = barrier timeout)
+  int coop_blocks = 0;          // co-resident blocks for the persistent kernel
+  double* h_scal = nullptr;  // pinned host scalars (h_scal[8] holds the status word)
   int red_cap = 0;
   std::string err;
   bool cuda_failed = false;
@@ -147,6 +158,16 @@ void spmv(const Sell<VT>& M, const XT* x, XT* y, cudaStream_t s);
 // Chebyshev solve of M z = b with `ch` (deg products); work: 4 vectors of nrows
 template <typename VT, typename XT>
 void cheb_solve(const Sell<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s);
+// Same, all `deg` iterations in one cooperative launch with a bounded grid
+// barrier between iterations (for the small pressure system).  On a barrier
+// timeout the kernel sets *status = 1 and returns.
+template <typename VT, typename XT>
+void cheb_solve_persistent(const Sell<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, GridBar* bar,
+                           int* status, int blocks, cudaStream_t s);
+int coop_blocks_for_persistent();
+// Bring the sticky device status back (sync); returns NM_OK or NM_ERR_TIMEOUT.
+int check_status(nm_ctx* c);
+int upload_cheb(nm_ctx* c, ChebSetup& ch);
 // w = A_s v (+ E_s y); epilogue modes
 struct FiltEpi {
   int mode = 0;        // 0: out = w; 1: filter recurrence

@@ -3,6 +3,7 @@
 // FP64 vector / Gram-Schmidt kernels of the Lanczos process.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <type_traits>
 
@@ -40,7 +41,16 @@ __device__ __forceinline__ float fmaT<float>(float a, float b, float c) { return
 // Row product of one SELL row in CSR order.  Two accumulators keep two
 // independent FMA chains in flight; they are combined at the end so the
 // result is deterministic.
-template <typename VT, typename XT>
+// COHERENT_X: x was written earlier in the same launch by other blocks (the
+// persistent kernel), so it must not go through the non-coherent read-only
+// cache.
+template <typename XT, bool COHERENT_X>
+__device__ __forceinline__ XT ldx(const XT* p) {
+  if (COHERENT_X) return *p;
+  return __ldg(p);
+}
+
+template <typename VT, typename XT, bool COHERENT_X = false>
 __device__ __forceinline__ XT sell_row(const SellView<VT>& M, int row, const XT* __restrict__ x) {
   const long long base = M.slice_ptr[row >> 5] + (row & 31);
   const int len = M.row_len[row];
@@ -51,12 +61,12 @@ __device__ __forceinline__ XT sell_row(const SellView<VT>& M, int row, const XT*
     const long long e1 = e0 + kSlice;
     const int c0 = __ldg(M.col + e0), c1 = __ldg(M.col + e1);
     const VT v0 = __ldg(M.val + e0), v1 = __ldg(M.val + e1);
-    s0 = fmaT<XT>((XT)v0, __ldg(x + c0), s0);
-    s1 = fmaT<XT>((XT)v1, __ldg(x + c1), s1);
+    s0 = fmaT<XT>((XT)v0, ldx<XT, COHERENT_X>(x + c0), s0);
+    s1 = fmaT<XT>((XT)v1, ldx<XT, COHERENT_X>(x + c1), s1);
   }
   if (k < len) {
     const long long e0 = base + (long long)k * kSlice;
-    s0 = fmaT<XT>((XT)__ldg(M.val + e0), __ldg(x + __ldg(M.col + e0)), s0);
+    s0 = fmaT<XT>((XT)__ldg(M.val + e0), ldx<XT, COHERENT_X>(x + __ldg(M.col + e0)), s0);
   }
   return s0 + s1;
 }
@@ -98,6 +108,83 @@ __global__ void __launch_bounds__(kThreads)
     r[row] = rr;
     x[row] = xn;
     dnext[row] = dn;
+  }
+}
+
+// Bounded grid barrier (sense by generation counter).  Thread 0 of each block
+// arrives; the last arrival resets the counter and bumps the generation; the
+// others poll the generation with a spin limit.  Returns false (and sets
+// *status) if the wait gave up or another block already failed.
+__device__ __forceinline__ bool grid_barrier(GridBar* bar, unsigned nblocks, int* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned g = *((volatile unsigned*)&bar->gen);
+    __threadfence();
+    const unsigned arrived = atomicAdd(&bar->count, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(&bar->count, 0u);
+      __threadfence();
+      atomicAdd(&bar->gen, 1u);
+    } else {
+      long long spins = 0;
+      while (*((volatile unsigned*)&bar->gen) == g) {
+        if (*((volatile int*)status) != 0) {
+          ok = 0;
+          break;
+        }
+        if (++spins > kSpinLimit) {
+          atomicExch(status, 1);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// All `deg` Chebyshev iterations in one launch; rows in a grid-stride loop,
+// a grid barrier between iterations.  Same arithmetic per row as k_cheb.
+template <typename VT, typename XT>
+__global__ void __launch_bounds__(kThreads)
+    k_cheb_persist(SellView<VT> M, const XT* __restrict__ b, XT* xout, XT* r, XT* x, XT* d0, XT* d1,
+                   const double* __restrict__ coef,
+                   int deg, XT inv_theta, GridBar* bar, int* status) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int k = 0; k < deg; ++k) {
+    const XT a = (XT)coef[k], c = (XT)coef[deg + k];
+    const XT* dcur = (k & 1) ? d1 : d0;
+    XT* dnext = (k & 1) ? d0 : d1;
+    const bool first = k == 0, last = k == deg - 1;
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < M.nrows; row += stride) {
+      XT dc, rr, xn;
+      if (first) {
+        const XT t = sell_row<VT, XT>(M, row, b) * inv_theta;
+        const XT bi = b[row];
+        dc = bi * inv_theta;
+        rr = bi - t;
+        xn = dc;
+      } else {
+        const XT t = sell_row<VT, XT, true>(M, row, dcur);
+        dc = dcur[row];
+        rr = r[row] - t;
+        xn = x[row] + dc;
+      }
+      const XT dn = fmaT<XT>(a, dc, c * rr);
+      if (last) {
+        xout[row] = xn + dn;
+      } else {
+        r[row] = rr;
+        x[row] = xn;
+        dnext[row] = dn;
+      }
+    }
+    if (!last && !grid_barrier(bar, gridDim.x, status)) return;
   }
 }
 
@@ -349,6 +436,52 @@ template void cheb_solve<double, double>(const Sell<double>&, const ChebSetup&, 
                                          cudaStream_t);
 template void cheb_solve<float, float>(const Sell<float>&, const ChebSetup&, const float*, float*, float*,
                                        cudaStream_t);
+
+template <typename VT, typename XT>
+void cheb_solve_persistent(const Sell<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, GridBar* bar,
+                           int* status, int blocks, cudaStream_t s) {
+  const int n = M.nrows;
+  if (n == 0 || ch.deg == 0) return;
+  XT* r = work;
+  XT* d0 = work + n;
+  XT* d1 = work + 2 * (size_t)n;
+  XT* xi = work + 3 * (size_t)n;
+  const SellView<VT> v = view(M);
+  const XT it = (XT)ch.inv_theta;
+  const double* coef = ch.d_coef;
+  int deg = ch.deg;
+  blocks = std::min(blocks, nblk(n));
+  if (blocks < 1) blocks = 1;
+  cudaMemsetAsync(bar, 0, sizeof(GridBar), s);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_cheb_persist<VT, XT>, v, b, x, r, xi, d0, d1, coef, deg, it, bar, status);
+}
+template void cheb_solve_persistent<double, double>(const Sell<double>&, const ChebSetup&, const double*, double*,
+                                                    double*, GridBar*, int*, int, cudaStream_t);
+template void cheb_solve_persistent<float, float>(const Sell<float>&, const ChebSetup&, const float*, float*, float*,
+                                                  GridBar*, int*, int, cudaStream_t);
+
+int coop_blocks_for_persistent() {
+  int dev = 0, sms = 0, per = 0, coop = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  if (!coop) return 0;
+  int p64 = 0, p32 = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p64, k_cheb_persist<double, double>, kThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p32, k_cheb_persist<float, float>, kThreads, 0);
+  per = std::min(p64, p32);
+  return per * sms;
+}
 
 template <typename VT, typename XT>
 void amv_fused(const Sell<VT>& A, const Sell<VT>* E, const XT* v, const XT* y, XT* out, const XT* vk, const XT* vkm1,

@@ -79,10 +79,17 @@ __global__ void k_resid(const double* __restrict__ w, const double* __restrict__
 double dot_sync(nm_ctx* c, const double* x, const double* y, int n) {
   dev_dot(x, y, n, c->red, c->scal, c->stream);
   cudaError_t e = cudaMemcpyAsync(c->h_scal, c->scal, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->h_scal + 8, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) {
     c->cuda_failed = true;
     set_err(c, NM_ERR_CUDA, std::string("device error: ") + cudaGetErrorString(e));
+    return std::nan("");
+  }
+  if (*(int*)(c->h_scal + 8) != 0) {
+    c->cuda_failed = true;
+    set_err(c, NM_ERR_TIMEOUT, "a grid barrier of the persistent Chebyshev kernel timed out");
     return std::nan("");
   }
   return c->h_scal[0];
@@ -153,7 +160,8 @@ int lanczos_bounds(nm_ctx* c, int nn, const Apply& op, const Apply& solve, int m
     if (!std::isfinite(a) || !std::isfinite(b)) {
       free_basis(V);
       free_basis(Zb);
-      return c->cuda_failed ? NM_ERR_CUDA : set_err(c, NM_ERR_NUMERIC, "non-finite value in Lanczos bounds");
+      return c->cuda_failed ? (c->err.find("timed out") != std::string::npos ? NM_ERR_TIMEOUT : NM_ERR_CUDA)
+                           : set_err(c, NM_ERR_NUMERIC, "non-finite value in Lanczos bounds");
     }
     beta.push_back(b);
     const bool last = (k == msteps - 1) || b == 0.0;
@@ -194,7 +202,10 @@ void chebav_t(nm_ctx* c, const Sell<VT>& A, const Sell<VT>& Bm, const Sell<VT>& 
     cheb_solve<VT, XT>(Bm, c->chebB, vk, w2, bwork, s);
     if (c->fs) {
       spmv<VT, XT>(ETm, w2, x0, s);
-      cheb_solve<VT, XT>(Apm, c->chebAp, x0, y0, apwork, s);
+      if (c->coop_blocks > 0)
+        cheb_solve_persistent<VT, XT>(Apm, c->chebAp, x0, y0, apwork, c->bar, c->d_status, c->coop_blocks, s);
+      else
+        cheb_solve<VT, XT>(Apm, c->chebAp, x0, y0, apwork, s);
     }
     FiltEpi ep;
     ep.mode = 1;
@@ -256,7 +267,11 @@ void amv64(nm_ctx* c, const double* x, double* y) {
   FiltEpi ep;
   if (c->fs) {
     spmv<double, double>(c->ET, x, c->w[12], c->stream);
-    cheb_solve<double, double>(c->Ap, c->chebAp, c->w[12], c->w[13], c->w[14], c->stream);
+    if (c->coop_blocks > 0)
+      cheb_solve_persistent<double, double>(c->Ap, c->chebAp, c->w[12], c->w[13], c->w[14], c->bar, c->d_status,
+                                            c->coop_blocks, c->stream);
+    else
+      cheb_solve<double, double>(c->Ap, c->chebAp, c->w[12], c->w[13], c->w[14], c->stream);
     amv_fused<double, double>(c->A, &c->E, x, c->w[13], y, nullptr, nullptr, nullptr, ep, c->stream);
     c->n_spmv += 2 + c->chebAp.deg;
   } else {
@@ -276,7 +291,11 @@ void filter_step64(nm_ctx* c, const double* vk, double* vkm1, double* vkp1, doub
   cheb_solve<double, double>(c->B, c->chebB, vk, c->w[11], c->w[4], c->stream);
   if (c->fs) {
     spmv<double, double>(c->ET, c->w[11], c->w[12], c->stream);
-    cheb_solve<double, double>(c->Ap, c->chebAp, c->w[12], c->w[13], c->w[14], c->stream);
+    if (c->coop_blocks > 0)
+      cheb_solve_persistent<double, double>(c->Ap, c->chebAp, c->w[12], c->w[13], c->w[14], c->bar, c->d_status,
+                                            c->coop_blocks, c->stream);
+    else
+      cheb_solve<double, double>(c->Ap, c->chebAp, c->w[12], c->w[13], c->w[14], c->stream);
   }
   FiltEpi ep;
   ep.mode = 1;
@@ -435,7 +454,8 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
     beta = std::sqrt(std::max(dot_sync(c, vnew, znew, n), 0.0));
     if (!std::isfinite(alpha) || !std::isfinite(beta)) {
       if (gexec) cudaGraphExecDestroy(gexec);
-      return c->cuda_failed ? NM_ERR_CUDA : set_err(c, NM_ERR_NUMERIC, "non-finite Lanczos coefficient");
+      return c->cuda_failed ? (c->err.find("timed out") != std::string::npos ? NM_ERR_TIMEOUT : NM_ERR_CUDA)
+                            : set_err(c, NM_ERR_NUMERIC, "non-finite Lanczos coefficient");
     }
     kdim = k + 1;
     if (beta == 0.0) {
@@ -531,6 +551,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
   cudaFree(U);
   cudaFree(dS);
   NM_CUDA(c, cudaGetLastError());
+  if ((rc = check_status(c))) return rc;
   const double t4 = now_s();
   res->t_bounds = t1 - t0;
   res->t_filter_design = t2 - t1;
