@@ -76,6 +76,8 @@ typedef struct {
   int want_vectors;   /* copy eigenvectors to the result                           */
   int unscale;        /* vectors as x = y .* D (src/mod_pevsl.f90:199) not y       */
   int use_graph;      /* capture the filter in a CUDA graph (default on)           */
+  int block;          /* 0/1: single-vector ChebLanNr (the reference's algorithm);
+                         32: block filtered Lanczos, 32 vectors per filter pass  */
 } nm_solve_opts;
 
 typedef struct {

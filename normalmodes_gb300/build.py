@@ -101,7 +101,7 @@ def build_gpu(force: bool = False, verbose_ptxas: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
         list(ex.map(_run, jobs))
     _run([nvcc] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", out] + objs +
-         ["-lcudart", "-lgomp"])
+         ["-lcudart", "-lcublas", "-lcusolver", "-lgomp"])
     return out
 
 

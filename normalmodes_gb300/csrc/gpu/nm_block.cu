@@ -1,0 +1,598 @@
+// Grouped 3-component operators and the block (32-column) SpMM kernels of
+// the batched filtered Lanczos.  See nm_block.h for the layout.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <type_traits>
+
+#include "nm_block.h"
+
+namespace nmg {
+
+// ---------------------------------------------------------------- host extraction
+namespace {
+inline bool same_row_pattern(const nm_csr* m, int r0, int r1, int colshift) {
+  const int l0 = m->rowptr[r0 + 1] - m->rowptr[r0], l1 = m->rowptr[r1 + 1] - m->rowptr[r1];
+  if (l0 != l1) return false;
+  for (int k = 0; k < l0; ++k)
+    if (m->col[m->rowptr[r1] + k] != m->col[m->rowptr[r0] + k] + colshift) return false;
+  return true;
+}
+}  // namespace
+
+bool group_mass(const nm_csr* B, const std::vector<double>& D, GCsrHost& M) {
+  if (B->nrows % 3) return false;
+  const int ng = B->nrows / 3;
+  M = GCsrHost();
+  M.nrows = M.ncols = ng;
+  M.bs = 1;
+  M.rp.assign(ng + 1, 0);
+  for (int g = 0; g < ng; ++g) {
+    for (int p = 1; p < 3; ++p) {
+      if (!same_row_pattern(B, 3 * g, 3 * g + p, p)) return false;
+      if (D[3 * g + p] != D[3 * g]) return false;
+      for (int k = 0; k < B->rowptr[3 * g + 1] - B->rowptr[3 * g]; ++k)
+        if (B->val[B->rowptr[3 * g + p] + k] != B->val[B->rowptr[3 * g] + k]) return false;
+    }
+    for (int q = B->rowptr[3 * g]; q < B->rowptr[3 * g + 1]; ++q) {
+      const int c = B->col[q];
+      if (c % 3) return false;
+      M.ci.push_back(c / 3);
+      M.v.push_back(B->val[q] * D[c] * D[3 * g]);
+    }
+    M.rp[g + 1] = (int)M.ci.size();
+  }
+  return true;
+}
+
+bool group_bsr3(const nm_csr* A, const std::vector<double>& dl, const std::vector<double>& dr, GCsrHost& G) {
+  if (A->nrows % 3 || A->ncols % 3) return false;
+  const int ng = A->nrows / 3;
+  G = GCsrHost();
+  G.nrows = ng;
+  G.ncols = A->ncols / 3;
+  G.bs = 9;
+  G.rp.assign(ng + 1, 0);
+  for (int g = 0; g < ng; ++g) {
+    for (int p = 1; p < 3; ++p)
+      if (!same_row_pattern(A, 3 * g, 3 * g + p, 0)) return false;
+    const int q0 = A->rowptr[3 * g], len = A->rowptr[3 * g + 1] - q0;
+    if (len % 3) return false;
+    for (int k = 0; k < len; k += 3) {
+      const int c = A->col[q0 + k];
+      if (c % 3 || A->col[q0 + k + 1] != c + 1 || A->col[q0 + k + 2] != c + 2) return false;
+      G.ci.push_back(c / 3);
+      for (int p = 0; p < 3; ++p)
+        for (int q = 0; q < 3; ++q) {
+          const int r = 3 * g + p;
+          G.v.push_back(A->val[A->rowptr[r] + k + q] * dr[c + q] * dl[r]);
+        }
+    }
+    G.rp[g + 1] = (int)G.ci.size();
+  }
+  return true;
+}
+
+bool group_e(const nm_csr* E, const std::vector<double>& D, const std::vector<double>& Dp, GCsrHost& G) {
+  if (E->nrows % 3) return false;
+  const int ng = E->nrows / 3;
+  G = GCsrHost();
+  G.nrows = ng;
+  G.ncols = E->ncols;
+  G.bs = 3;
+  G.rp.assign(ng + 1, 0);
+  for (int g = 0; g < ng; ++g) {
+    for (int p = 1; p < 3; ++p)
+      if (!same_row_pattern(E, 3 * g, 3 * g + p, 0)) return false;
+    const int len = E->rowptr[3 * g + 1] - E->rowptr[3 * g];
+    for (int k = 0; k < len; ++k) {
+      const int c = E->col[E->rowptr[3 * g] + k];
+      G.ci.push_back(c);
+      for (int p = 0; p < 3; ++p) {
+        const int r = 3 * g + p;
+        G.v.push_back(E->val[E->rowptr[r] + k] * Dp[c] * D[r]);
+      }
+    }
+    G.rp[g + 1] = (int)G.ci.size();
+  }
+  return true;
+}
+
+bool group_et(const nm_csr* ET, const std::vector<double>& Dp, const std::vector<double>& D, GCsrHost& G) {
+  if (ET->ncols % 3) return false;
+  G = GCsrHost();
+  G.nrows = ET->nrows;
+  G.ncols = ET->ncols / 3;
+  G.bs = 3;
+  G.rp.assign(ET->nrows + 1, 0);
+  for (int r = 0; r < ET->nrows; ++r) {
+    const int q0 = ET->rowptr[r], len = ET->rowptr[r + 1] - q0;
+    if (len % 3) return false;
+    for (int k = 0; k < len; k += 3) {
+      const int c = ET->col[q0 + k];
+      if (c % 3 || ET->col[q0 + k + 1] != c + 1 || ET->col[q0 + k + 2] != c + 2) return false;
+      G.ci.push_back(c / 3);
+      for (int q = 0; q < 3; ++q) G.v.push_back(ET->val[q0 + k + q] * D[c + q] * Dp[r]);
+    }
+    G.rp[r + 1] = (int)G.ci.size();
+  }
+  return true;
+}
+
+void scalar_csr(const nm_csr* m, const std::vector<double>& dl, const std::vector<double>& dr, double sign,
+                GCsrHost& G) {
+  G = GCsrHost();
+  G.nrows = m->nrows;
+  G.ncols = m->ncols;
+  G.bs = 1;
+  G.rp.assign(m->rowptr, m->rowptr + m->nrows + 1);
+  G.ci.assign(m->col, m->col + m->rowptr[m->nrows]);
+  G.v.resize(G.ci.size());
+  for (int r = 0; r < m->nrows; ++r)
+    for (int q = m->rowptr[r]; q < m->rowptr[r + 1]; ++q) G.v[q] = sign * m->val[q] * dr[m->col[q]] * dl[r];
+}
+
+template <typename T>
+int upload_g(nm_ctx* c, const GCsrHost& h, GCsr<T>& d) {
+  free_g(d);
+  d.nrows = h.nrows;
+  d.ncols = h.ncols;
+  d.bs = h.bs;
+  d.nnz = (long long)h.ci.size();
+  NM_CUDA(c, cudaMalloc(&d.rp, sizeof(int) * (h.nrows + 1)));
+  NM_CUDA(c, cudaMalloc(&d.ci, sizeof(int) * std::max<long long>(d.nnz, 1)));
+  NM_CUDA(c, cudaMalloc(&d.v, sizeof(T) * std::max<size_t>(h.v.size(), 1)));
+  NM_CUDA(c, cudaMemcpy(d.rp, h.rp.data(), sizeof(int) * (h.nrows + 1), cudaMemcpyHostToDevice));
+  if (d.nnz) NM_CUDA(c, cudaMemcpy(d.ci, h.ci.data(), sizeof(int) * d.nnz, cudaMemcpyHostToDevice));
+  if (!h.v.empty()) {
+    if (std::is_same<T, double>::value) {
+      NM_CUDA(c, cudaMemcpy(d.v, h.v.data(), sizeof(double) * h.v.size(), cudaMemcpyHostToDevice));
+    } else {
+      std::vector<T> tmp(h.v.begin(), h.v.end());
+      NM_CUDA(c, cudaMemcpy(d.v, tmp.data(), sizeof(T) * tmp.size(), cudaMemcpyHostToDevice));
+    }
+  }
+  c->dev_bytes += d.bytes();
+  return NM_OK;
+}
+template int upload_g<double>(nm_ctx*, const GCsrHost&, GCsr<double>&);
+template int upload_g<float>(nm_ctx*, const GCsrHost&, GCsr<float>&);
+
+template <typename T>
+void free_g(GCsr<T>& g) {
+  cudaFree(g.rp);
+  cudaFree(g.ci);
+  cudaFree(g.v);
+  g = GCsr<T>();
+}
+template void free_g<double>(GCsr<double>&);
+template void free_g<float>(GCsr<float>&);
+
+// ---------------------------------------------------------------- kernels
+namespace {
+
+constexpr int kT = 256;             // threads per block = 8 rows of 32 lanes
+constexpr int kRowsPerBlock = kT / kBlk;
+inline int nrb(long long rows) { return (int)((rows + kRowsPerBlock - 1) / kRowsPerBlock); }
+
+template <typename XT>
+__device__ __forceinline__ XT fm(XT a, XT b, XT c) {
+  return fma(a, b, c);
+}
+
+template <typename XT, bool COH>
+__device__ __forceinline__ XT ld(const XT* p) {
+  if (COH) return *p;
+  return __ldg(p);
+}
+
+// One Chebyshev iteration of the mass solve on a block: rows are 3-DOF
+// groups, t_p = sum_h M_gh x(3h+p, lane).
+template <typename VT, typename XT, bool FIRST, bool LAST>
+__global__ void __launch_bounds__(kT)
+    k_mass_cheb(int ng, const int* __restrict__ rp, const int* __restrict__ ci, const VT* __restrict__ mv,
+                const XT* __restrict__ b, XT* __restrict__ x, XT* __restrict__ r, const XT* __restrict__ dcur,
+                XT* __restrict__ dnext, XT* __restrict__ xout, XT a, XT c, XT inv_theta) {
+  const int lane = threadIdx.x & (kBlk - 1);
+  const int g = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5);
+  if (g >= ng) return;
+  const XT* src = FIRST ? b : dcur;
+  XT t0 = 0, t1 = 0, t2 = 0;
+  const int e1 = rp[g + 1];
+  for (int e = rp[g]; e < e1; ++e) {
+    const int h = __ldg(ci + e);
+    const XT m = (XT)__ldg(mv + e);
+    const XT* xs = src + (size_t)3 * h * kBlk + lane;
+    t0 = fm<XT>(m, __ldg(xs), t0);
+    t1 = fm<XT>(m, __ldg(xs + kBlk), t1);
+    t2 = fm<XT>(m, __ldg(xs + 2 * kBlk), t2);
+  }
+  const XT tt[3] = {t0, t1, t2};
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    const size_t idx = ((size_t)3 * g + p) * kBlk + lane;
+    XT dc, rr, xn;
+    if (FIRST) {
+      const XT bi = b[idx];
+      dc = bi * inv_theta;
+      rr = bi - tt[p] * inv_theta;
+      xn = dc;
+    } else {
+      dc = dcur[idx];
+      rr = r[idx] - tt[p];
+      xn = x[idx] + dc;
+    }
+    const XT dn = fm<XT>(a, dc, c * rr);
+    if (LAST) {
+      xout[idx] = xn + dn;
+    } else {
+      r[idx] = rr;
+      x[idx] = xn;
+      dnext[idx] = dn;
+    }
+  }
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(kT) k_mass_spmv(int ng, const int* __restrict__ rp, const int* __restrict__ ci,
+                                                  const VT* __restrict__ mv, const double* __restrict__ x,
+                                                  double* __restrict__ y) {
+  const int lane = threadIdx.x & (kBlk - 1);
+  const int g = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5);
+  if (g >= ng) return;
+  double t0 = 0, t1 = 0, t2 = 0;
+  for (int e = rp[g]; e < rp[g + 1]; ++e) {
+    const int h = __ldg(ci + e);
+    const double m = (double)__ldg(mv + e);
+    const double* xs = x + (size_t)3 * h * kBlk + lane;
+    t0 = fma(m, __ldg(xs), t0);
+    t1 = fma(m, __ldg(xs + kBlk), t1);
+    t2 = fma(m, __ldg(xs + 2 * kBlk), t2);
+  }
+  y[((size_t)3 * g) * kBlk + lane] = t0;
+  y[((size_t)3 * g + 1) * kBlk + lane] = t1;
+  y[((size_t)3 * g + 2) * kBlk + lane] = t2;
+}
+
+// x0(k, lane) = sum_entries sum_q et_q w(3h+q, lane)   (pressure rows)
+template <typename VT, typename XT>
+__global__ void __launch_bounds__(kT) k_et(int np, const int* __restrict__ rp, const int* __restrict__ ci,
+                                           const VT* __restrict__ v3, const XT* __restrict__ w, XT* __restrict__ x0) {
+  const int lane = threadIdx.x & (kBlk - 1);
+  const int k = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5);
+  if (k >= np) return;
+  XT s = 0;
+  for (int e = rp[k]; e < rp[k + 1]; ++e) {
+    const int h = __ldg(ci + e);
+    const XT* ws = w + (size_t)3 * h * kBlk + lane;
+    s = fm<XT>((XT)__ldg(v3 + 3 * (size_t)e), __ldg(ws), s);
+    s = fm<XT>((XT)__ldg(v3 + 3 * (size_t)e + 1), __ldg(ws + kBlk), s);
+    s = fm<XT>((XT)__ldg(v3 + 3 * (size_t)e + 2), __ldg(ws + 2 * kBlk), s);
+  }
+  x0[(size_t)k * kBlk + lane] = s;
+}
+
+__device__ __forceinline__ bool gbar(GridBar* bar, unsigned nblocks, int* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned g = *((volatile unsigned*)&bar->gen);
+    __threadfence();
+    if (atomicAdd(&bar->count, 1u) == nblocks - 1) {
+      atomicExch(&bar->count, 0u);
+      __threadfence();
+      atomicAdd(&bar->gen, 1u);
+    } else {
+      long long spins = 0;
+      while (*((volatile unsigned*)&bar->gen) == g) {
+        if (*((volatile int*)status) != 0) {
+          ok = 0;
+          break;
+        }
+        if (++spins > kSpinLimit) {
+          atomicExch(status, 1);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Persistent Chebyshev solve on the pressure block: all iterations in one
+// cooperative launch, rows in a grid-stride loop, bounded grid barriers.
+template <typename VT, typename XT>
+__global__ void __launch_bounds__(kT)
+    k_ap_cheb(int np, const int* __restrict__ rp, const int* __restrict__ ci, const VT* __restrict__ av,
+              const XT* __restrict__ b, XT* xout, XT* r, XT* x, XT* d0, XT* d1, const double* __restrict__ coef,
+              int deg, XT inv_theta, GridBar* bar, int* status) {
+  const int lane = threadIdx.x & (kBlk - 1);
+  const int rstride = gridDim.x * kRowsPerBlock;
+  for (int k = 0; k < deg; ++k) {
+    const XT a = (XT)coef[k], c = (XT)coef[deg + k];
+    const XT* dcur = (k & 1) ? d1 : d0;
+    XT* dnext = (k & 1) ? d0 : d1;
+    const bool first = k == 0, last = k == deg - 1;
+    for (int row = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5); row < np; row += rstride) {
+      const XT* src = first ? b : dcur;
+      XT t = 0;
+      for (int e = rp[row]; e < rp[row + 1]; ++e) {
+        const int h = __ldg(ci + e);
+        t = fm<XT>((XT)__ldg(av + e), first ? __ldg(src + (size_t)h * kBlk + lane) : src[(size_t)h * kBlk + lane], t);
+      }
+      const size_t idx = (size_t)row * kBlk + lane;
+      XT dc, rr, xn;
+      if (first) {
+        const XT bi = b[idx];
+        dc = bi * inv_theta;
+        rr = bi - t * inv_theta;
+        xn = dc;
+      } else {
+        dc = dcur[idx];
+        rr = r[idx] - t;
+        xn = x[idx] + dc;
+      }
+      const XT dn = fm<XT>(a, dc, c * rr);
+      if (last) {
+        xout[idx] = xn + dn;
+      } else {
+        r[idx] = rr;
+        x[idx] = xn;
+        dnext[idx] = dn;
+      }
+    }
+    if (!last && !gbar(bar, gridDim.x, status)) return;
+  }
+}
+
+// w(3g+p) = sum_h A_gh(p, :) v(3h + :) [+ sum_k E_gk(p) y(k)]; epilogue as k_amv.
+template <typename VT, typename XT, bool HAS_E, int MODE>
+__global__ void __launch_bounds__(kT)
+    k_amv3(int ng, const int* __restrict__ arp, const int* __restrict__ aci, const VT* __restrict__ av,
+           const int* __restrict__ erp, const int* __restrict__ eci, const VT* __restrict__ ev,
+           const XT* __restrict__ v, const XT* __restrict__ y, XT* __restrict__ out, const XT* __restrict__ vk,
+           const XT* __restrict__ vkm1, XT* __restrict__ yacc, XT s, XT cc, XT pm, XT mu) {
+  const int lane = threadIdx.x & (kBlk - 1);
+  const int g = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5);
+  if (g >= ng) return;
+  XT w0 = 0, w1 = 0, w2 = 0;
+  for (int e = arp[g]; e < arp[g + 1]; ++e) {
+    const int h = __ldg(aci + e);
+    const XT* vs = v + (size_t)3 * h * kBlk + lane;
+    const XT x0 = __ldg(vs), x1 = __ldg(vs + kBlk), x2 = __ldg(vs + 2 * kBlk);
+    const VT* a9 = av + 9 * (size_t)e;
+    w0 = fm<XT>((XT)__ldg(a9 + 0), x0, w0);
+    w0 = fm<XT>((XT)__ldg(a9 + 1), x1, w0);
+    w0 = fm<XT>((XT)__ldg(a9 + 2), x2, w0);
+    w1 = fm<XT>((XT)__ldg(a9 + 3), x0, w1);
+    w1 = fm<XT>((XT)__ldg(a9 + 4), x1, w1);
+    w1 = fm<XT>((XT)__ldg(a9 + 5), x2, w1);
+    w2 = fm<XT>((XT)__ldg(a9 + 6), x0, w2);
+    w2 = fm<XT>((XT)__ldg(a9 + 7), x1, w2);
+    w2 = fm<XT>((XT)__ldg(a9 + 8), x2, w2);
+  }
+  if (HAS_E) {
+    for (int e = erp[g]; e < erp[g + 1]; ++e) {
+      const XT yk = __ldg(y + (size_t)__ldg(eci + e) * kBlk + lane);
+      const VT* e3 = ev + 3 * (size_t)e;
+      w0 = fm<XT>((XT)__ldg(e3 + 0), yk, w0);
+      w1 = fm<XT>((XT)__ldg(e3 + 1), yk, w1);
+      w2 = fm<XT>((XT)__ldg(e3 + 2), yk, w2);
+    }
+  }
+  const XT ww[3] = {w0, w1, w2};
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    const size_t idx = ((size_t)3 * g + p) * kBlk + lane;
+    if (MODE == 0) {
+      out[idx] = ww[p];
+    } else {
+      const XT t = fm<XT>(s, fm<XT>(-cc, vk[idx], ww[p]), -pm * vkm1[idx]);
+      out[idx] = t;
+      yacc[idx] = fm<XT>(mu, t, yacc[idx]);
+    }
+  }
+}
+
+// blk(i, c) = Z(:, j0 + c)(i) through a 32 x 32 shared-memory tile.
+template <typename XT>
+__global__ void k_gather_cols(double* const* __restrict__ chunks, size_t ld, int j0, int n, XT* __restrict__ blk) {
+  __shared__ double tile[kBlk][kBlk + 1];
+  const int i0 = blockIdx.x * kBlk;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int c = ty; c < kBlk; c += 8) {
+    const int j = j0 + c;
+    const double* col = chunks[j / Basis::kChunk] + (size_t)(j % Basis::kChunk) * ld;
+    const int i = i0 + tx;
+    tile[c][tx] = i < n ? col[i] : 0.0;
+  }
+  __syncthreads();
+  for (int r = ty; r < kBlk; r += 8) {
+    const int i = i0 + r;
+    if (i < n) blk[(size_t)i * kBlk + tx] = (XT)tile[tx][r];
+  }
+}
+
+template <typename XT>
+__global__ void k_to_colmajor(const XT* __restrict__ blk, int n, double* __restrict__ out, size_t ld) {
+  __shared__ double tile[kBlk][kBlk + 1];
+  const int i0 = blockIdx.x * kBlk;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int r = ty; r < kBlk; r += 8) {
+    const int i = i0 + r;
+    tile[r][tx] = i < n ? (double)blk[(size_t)i * kBlk + tx] : 0.0;
+  }
+  __syncthreads();
+  for (int c = ty; c < kBlk; c += 8) {
+    const int i = i0 + tx;
+    if (i < n) out[(size_t)c * ld + i] = tile[tx][c];
+  }
+}
+
+template <typename XT>
+__global__ void k_from_colmajor(const double* __restrict__ src, size_t ld, int n, XT* __restrict__ blk) {
+  __shared__ double tile[kBlk][kBlk + 1];
+  const int i0 = blockIdx.x * kBlk;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int c = ty; c < kBlk; c += 8) {
+    const int i = i0 + tx;
+    tile[c][tx] = i < n ? src[(size_t)c * ld + i] : 0.0;
+  }
+  __syncthreads();
+  for (int r = ty; r < kBlk; r += 8) {
+    const int i = i0 + r;
+    if (i < n) blk[(size_t)i * kBlk + tx] = (XT)tile[tx][r];
+  }
+}
+
+template <typename XT>
+__global__ void k_init_filter_blk(XT* vk, XT* vkm1, XT* y, const XT* v, XT mu0, size_t len) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < len) {
+    const XT vi = v[i];
+    vk[i] = vi;
+    vkm1[i] = 0;
+    y[i] = mu0 * vi;
+  }
+}
+
+}  // namespace
+
+template <typename VT, typename XT>
+void blk_mass_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s) {
+  const int ng = M.nrows;
+  const size_t len = (size_t)3 * ng * kBlk;
+  XT* r = work;
+  XT* d0 = work + len;
+  XT* d1 = work + 2 * len;
+  XT* xi = work + 3 * len;
+  const XT it = (XT)ch.inv_theta;
+  for (int k = 0; k < ch.deg; ++k) {
+    const XT a = (XT)ch.a[k], c = (XT)ch.c[k];
+    const bool first = k == 0, last = k == ch.deg - 1;
+    XT* dcur = (k & 1) ? d1 : d0;
+    XT* dnext = (k & 1) ? d0 : d1;
+#define NM_MC(F, L) \
+  k_mass_cheb<VT, XT, F, L><<<nrb(ng), kT, 0, s>>>(ng, M.rp, M.ci, M.v, b, xi, r, dcur, dnext, x, a, c, it)
+    if (first && last) NM_MC(true, true);
+    else if (first) NM_MC(true, false);
+    else if (last) NM_MC(false, true);
+    else NM_MC(false, false);
+#undef NM_MC
+  }
+}
+
+template <typename VT>
+void blk_mass_spmv(const GCsr<VT>& M, const double* x, double* y, cudaStream_t s) {
+  k_mass_spmv<VT><<<nrb(M.nrows), kT, 0, s>>>(M.nrows, M.rp, M.ci, M.v, x, y);
+}
+
+template <typename VT, typename XT>
+void blk_et(const GCsr<VT>& ET, const XT* w, XT* x0, cudaStream_t s) {
+  k_et<VT, XT><<<nrb(ET.nrows), kT, 0, s>>>(ET.nrows, ET.rp, ET.ci, ET.v, w, x0);
+}
+
+template <typename VT, typename XT>
+void blk_ap_cheb_persistent(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b, XT* x, XT* work, GridBar* bar,
+                            int* status, int blocks, cudaStream_t s) {
+  const int np = Ap.nrows;
+  if (np == 0 || ch.deg == 0) return;
+  const size_t len = (size_t)np * kBlk;
+  XT* r = work;
+  XT* d0 = work + len;
+  XT* d1 = work + 2 * len;
+  XT* xi = work + 3 * len;
+  blocks = std::max(1, std::min(blocks, nrb(np)));
+  cudaMemsetAsync(bar, 0, sizeof(GridBar), s);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(kT);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const XT it = (XT)ch.inv_theta;
+  int deg = ch.deg;
+  cudaLaunchKernelEx(&cfg, k_ap_cheb<VT, XT>, np, (const int*)Ap.rp, (const int*)Ap.ci, (const VT*)Ap.v, b, x, r, xi,
+                     d0, d1, (const double*)ch.d_coef, deg, it, bar, status);
+}
+
+int blk_coop_blocks() {
+  int dev = 0, sms = 0, coop = 0, p64 = 0, p32 = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  if (!coop) return 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p64, k_ap_cheb<double, double>, kT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p32, k_ap_cheb<float, float>, kT, 0);
+  return std::min(p64, p32) * sms;
+}
+
+template <typename VT, typename XT>
+void blk_amv(const GCsr<VT>& A, const GCsr<VT>* E, const XT* v, const XT* y, XT* out, const XT* vk, const XT* vkm1,
+             XT* yacc, const FiltEpi& ep, cudaStream_t s) {
+  const int ng = A.nrows;
+  const XT S = (XT)ep.s, CC = (XT)ep.cc, PM = (XT)ep.pm, MU = (XT)ep.mu;
+  const int* erp = E ? E->rp : nullptr;
+  const int* eci = E ? E->ci : nullptr;
+  const VT* ev = E ? E->v : nullptr;
+#define NM_AMV(HE, MO)                                                                                            \
+  k_amv3<VT, XT, HE, MO><<<nrb(ng), kT, 0, s>>>(ng, A.rp, A.ci, A.v, erp, eci, ev, v, y, out, vk, vkm1, yacc, S, \
+                                                CC, PM, MU)
+  if (E) {
+    if (ep.mode == 0) NM_AMV(true, 0);
+    else NM_AMV(true, 1);
+  } else {
+    if (ep.mode == 0) NM_AMV(false, 0);
+    else NM_AMV(false, 1);
+  }
+#undef NM_AMV
+}
+
+template <typename XT>
+void blk_gather_cols(const Basis& Z, int j0, int n, XT* blk, cudaStream_t s) {
+  k_gather_cols<XT><<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(Z.d_chunks, Z.ld, j0, n, blk);
+}
+template <typename XT>
+void blk_to_colmajor(const XT* blk, int n, double* out, size_t ld, cudaStream_t s) {
+  k_to_colmajor<XT><<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(blk, n, out, ld);
+}
+template <typename XT>
+void blk_from_colmajor(const double* src, size_t ld, int n, XT* blk, cudaStream_t s) {
+  k_from_colmajor<XT><<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(src, ld, n, blk);
+}
+template void blk_from_colmajor<float>(const double*, size_t, int, float*, cudaStream_t);
+template void blk_from_colmajor<double>(const double*, size_t, int, double*, cudaStream_t);
+
+template <typename XT>
+void blk_init_filter(XT* vk, XT* vkm1, XT* y, const XT* v, double mu0, size_t len, cudaStream_t s) {
+  k_init_filter_blk<XT><<<(int)((len + 255) / 256), 256, 0, s>>>(vk, vkm1, y, v, (XT)mu0, len);
+}
+
+#define NM_INST(VT, XT)                                                                                              \
+  template void blk_mass_cheb<VT, XT>(const GCsr<VT>&, const ChebSetup&, const XT*, XT*, XT*, cudaStream_t);        \
+  template void blk_et<VT, XT>(const GCsr<VT>&, const XT*, XT*, cudaStream_t);                                     \
+  template void blk_ap_cheb_persistent<VT, XT>(const GCsr<VT>&, const ChebSetup&, const XT*, XT*, XT*, GridBar*,   \
+                                               int*, int, cudaStream_t);                                           \
+  template void blk_amv<VT, XT>(const GCsr<VT>&, const GCsr<VT>*, const XT*, const XT*, XT*, const XT*, const XT*, \
+                                XT*, const FiltEpi&, cudaStream_t);
+NM_INST(double, double)
+NM_INST(float, float)
+#undef NM_INST
+template void blk_mass_spmv<double>(const GCsr<double>&, const double*, double*, cudaStream_t);
+template void blk_gather_cols<float>(const Basis&, int, int, float*, cudaStream_t);
+template void blk_gather_cols<double>(const Basis&, int, int, double*, cudaStream_t);
+template void blk_to_colmajor<float>(const float*, int, double*, size_t, cudaStream_t);
+template void blk_to_colmajor<double>(const double*, int, double*, size_t, cudaStream_t);
+template void blk_init_filter<float>(float*, float*, float*, const float*, double, size_t, cudaStream_t);
+template void blk_init_filter<double>(double*, double*, double*, const double*, double, size_t, cudaStream_t);
+
+}  // namespace nmg

@@ -1,0 +1,99 @@
+// Block (multi-vector) operators of libnmgpu: the grouped 3-component
+// layouts and the SpMM kernels behind the batched filtered Lanczos.
+//
+// Layout: a block of S = 32 vectors is stored row-major (row i holds the 32
+// column values contiguously), so a warp owns one matrix row and its 32 lanes
+// own the 32 columns: every gathered neighbour row is one coalesced 128-byte
+// (FP32) or 256-byte (FP64) load, and each matrix entry is a broadcast.
+// The matrices use the displacement structure of the reference's assembly
+// (3 DOFs per node copy, src/mod_cg_create_matrix.f90:1372-1389,1720-1736):
+//   B  = M (x) I_3          -> scalar CSR M over 3-DOF groups
+//   A, Ad                    -> CSR of 3x3 blocks over groups
+//   E  (n x np)              -> CSR of 3x1 blocks, ET (np x n) -> 1x3 blocks
+#pragma once
+
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include "nm_internal.h"
+
+namespace nmg {
+
+constexpr int kBlk = 32;
+
+template <typename T>
+struct GCsr {  // grouped CSR on the device
+  int nrows = 0, ncols = 0, bs = 1;  // bs values per entry (1, 3 or 9)
+  long long nnz = 0;                 // entries (blocks)
+  int* rp = nullptr;
+  int* ci = nullptr;
+  T* v = nullptr;
+  size_t bytes() const { return (size_t)(nrows + 1) * 4 + (size_t)nnz * (4 + bs * sizeof(T)); }
+};
+
+struct GCsrHost {
+  int nrows = 0, ncols = 0, bs = 1;
+  std::vector<int> rp, ci;
+  std::vector<double> v;
+};
+
+// Host extraction from scaled DOF-level CSR; false if the structure is absent.
+bool group_mass(const nm_csr* B, const std::vector<double>& D, GCsrHost& M);
+bool group_bsr3(const nm_csr* A, const std::vector<double>& dl, const std::vector<double>& dr, GCsrHost& G);
+bool group_e(const nm_csr* E, const std::vector<double>& D, const std::vector<double>& Dp, GCsrHost& G);
+bool group_et(const nm_csr* ET, const std::vector<double>& Dp, const std::vector<double>& D, GCsrHost& G);
+void scalar_csr(const nm_csr* m, const std::vector<double>& dl, const std::vector<double>& dr, double sign,
+                GCsrHost& G);
+
+template <typename T>
+int upload_g(nm_ctx* c, const GCsrHost& h, GCsr<T>& d);
+template <typename T>
+void free_g(GCsr<T>& g);
+
+// Block kernels (S = kBlk columns, row-major blocks).
+template <typename VT, typename XT>
+void blk_mass_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s);
+template <typename VT, typename XT>
+void blk_et(const GCsr<VT>& ET, const XT* w, XT* x0, cudaStream_t s);
+template <typename VT, typename XT>
+void blk_ap_cheb_persistent(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b, XT* x, XT* work, GridBar* bar,
+                            int* status, int blocks, cudaStream_t s);
+template <typename VT, typename XT>
+void blk_amv(const GCsr<VT>& A, const GCsr<VT>* E, const XT* v, const XT* y, XT* out, const XT* vk, const XT* vkm1,
+             XT* yacc, const FiltEpi& ep, cudaStream_t s);
+template <typename VT>
+void blk_mass_spmv(const GCsr<VT>& M, const double* x, double* y, cudaStream_t s);
+// Conversions between basis columns (FP64, column-major chunks) and row-major blocks.
+template <typename XT>
+void blk_gather_cols(const Basis& Z, int j0, int n, XT* blk, cudaStream_t s);   // blk = Z(:, j0:j0+S)^T
+template <typename XT>
+void blk_to_colmajor(const XT* blk, int n, double* out, size_t ld, cudaStream_t s);  // out(:, c) = blk(:, c)
+template <typename XT>
+void blk_init_filter(XT* vk, XT* vkm1, XT* y, const XT* v, double mu0, size_t len, cudaStream_t s);
+template <typename XT>
+void blk_from_colmajor(const double* src, size_t ld, int n, XT* blk, cudaStream_t s);  // blk = src(:, 0:S)^T
+int blk_coop_blocks();
+
+// Grouped operators and buffers of the batched path.
+struct BlockState {
+  bool ok = false;
+  GCsr<double> M64, A64, E64, ET64, Ap64;
+  GCsr<float> M32, A32, E32, ET32, Ap32;
+  float* f32 = nullptr;
+  double* f64 = nullptr;
+  size_t f32_len = 0, f64_len = 0;
+  cublasHandle_t cublas = nullptr;
+  cusolverDnHandle_t cusolver = nullptr;
+  int coop = 0;
+};
+int block_build(nm_ctx* c, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, const nm_csr* E, const nm_csr* ET);
+void block_free(nm_ctx* c);
+// Block filtered Lanczos; on success U (n x nc, column-major, device, owned
+// by the caller) holds the Ritz vectors with p(theta) >= bar.
+int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double** U, int* nc, int* steps);
+// FP64 Rayleigh-Ritz on the columns of U (n x nc): U <- U Q with
+// (U^T A U) Q = (U^T B U) Q Theta.  Resolves the mixing of close Ritz pairs
+// left by an FP32 filter.
+int rayleigh_ritz64(nm_ctx* c, double** U, int nc);
+
+}  // namespace nmg

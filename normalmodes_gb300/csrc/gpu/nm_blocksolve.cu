@@ -1,0 +1,533 @@
+// Batched (block) polynomial-filtered Lanczos of libnmgpu.
+//
+// The filter p(A B~^-1) of pEVSL_CHEBLANNR_F90 (src/mod_pevsl.f90:122) is
+// applied to 32 Krylov vectors at once (one SpMM pass over A, B and Ap per
+// Chebyshev step instead of 32 SpMV passes), in FP32 for the mixed precision
+// mode or FP64.  The Lanczos recurrence, the full block Gram-Schmidt against
+// the basis (cuBLAS DGEMM), the B~^-1 inner product (FP64 block Chebyshev
+// solve) and the Rayleigh-Ritz of the block-tridiagonal T (cuSOLVER) stay in
+// FP64.  The convergence test is the reference's restricted-trace test on
+// the Ritz values above the filter bar.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "nm_block.h"
+#include "nm_ops.h"
+
+namespace nmg {
+
+namespace {
+
+#define CB(c, x)                                                                          \
+  do {                                                                                    \
+    cublasStatus_t s_ = (x);                                                              \
+    if (s_ != CUBLAS_STATUS_SUCCESS) return set_err((c), NM_ERR_CUDA, "cuBLAS failure: " #x); \
+  } while (0)
+#define CS(c, x)                                                                            \
+  do {                                                                                      \
+    cusolverStatus_t s_ = (x);                                                              \
+    if (s_ != CUSOLVER_STATUS_SUCCESS) return set_err((c), NM_ERR_CUDA, "cuSOLVER failure: " #x); \
+  } while (0)
+
+BlockState* bs(nm_ctx* c) { return (BlockState*)c->blk; }
+
+// Upper Cholesky G = R^T R of an S x S (column-major) matrix.  false if not SPD.
+bool chol_upper(const double* G, int s, std::vector<double>& R) {
+  R.assign((size_t)s * s, 0.0);
+  for (int j = 0; j < s; ++j) {
+    double d = G[(size_t)j * s + j];
+    for (int k = 0; k < j; ++k) d -= R[(size_t)j * s + k] * R[(size_t)j * s + k];
+    if (!(d > 0.0) || !std::isfinite(d)) return false;
+    const double rjj = std::sqrt(d);
+    R[(size_t)j * s + j] = rjj;
+    for (int i = j + 1; i < s; ++i) {
+      double v = 0.5 * (G[(size_t)i * s + j] + G[(size_t)j * s + i]);
+      for (int k = 0; k < j; ++k) v -= R[(size_t)j * s + k] * R[(size_t)i * s + k];
+      R[(size_t)i * s + j] = v / rjj;  // R(j, i), column-major
+    }
+  }
+  return true;
+}
+
+}  // namespace
+
+int block_build(nm_ctx* c, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, const nm_csr* E, const nm_csr* ET) {
+  auto* st = new BlockState();
+  c->blk = st;
+  GCsrHost hM, hA, hE, hET, hAp;
+  bool ok = group_mass(B, c->hD, hM) && group_bsr3(A, c->hD, c->hD, hA);
+  if (ok && c->fs) ok = group_e(E, c->hD, c->hDp, hE) && group_et(ET, c->hDp, c->hD, hET);
+  if (!ok) return NM_OK;  // no grouped structure: the block path is unavailable
+  if (c->fs) scalar_csr(Ap, c->hDp, c->hDp, -1.0, hAp);
+  int rc;
+  if ((rc = upload_g(c, hM, st->M64)) || (rc = upload_g(c, hA, st->A64))) return rc;
+  if (c->fs && ((rc = upload_g(c, hE, st->E64)) || (rc = upload_g(c, hET, st->ET64)) || (rc = upload_g(c, hAp, st->Ap64))))
+    return rc;
+  if (c->precision == NM_PREC_MIXED) {
+    if ((rc = upload_g(c, hM, st->M32)) || (rc = upload_g(c, hA, st->A32))) return rc;
+    if (c->fs &&
+        ((rc = upload_g(c, hE, st->E32)) || (rc = upload_g(c, hET, st->ET32)) || (rc = upload_g(c, hAp, st->Ap32))))
+      return rc;
+  }
+  st->coop = blk_coop_blocks();
+  st->ok = true;
+  return NM_OK;
+}
+
+void block_free(nm_ctx* c) {
+  BlockState* st = bs(c);
+  if (!st) return;
+  for (auto* g : {&st->M64, &st->A64, &st->E64, &st->ET64, &st->Ap64}) free_g(*g);
+  for (auto* g : {&st->M32, &st->A32, &st->E32, &st->ET32, &st->Ap32}) free_g(*g);
+  cudaFree(st->f32);
+  cudaFree(st->f64);
+  if (st->cublas) cublasDestroy(st->cublas);
+  if (st->cusolver) cusolverDnDestroy(st->cusolver);
+  delete st;
+  c->blk = nullptr;
+}
+
+namespace {
+
+template <typename XT>
+XT* carve(XT*& p, size_t len) {
+  XT* r = p;
+  p += len;
+  return r;
+}
+
+// Buffers of one block filter application in precision XT.
+template <typename XT>
+struct FiltBufs {
+  XT *zin, *yout, *vk, *vkm1, *vkp1, *w2, *bwork, *x0, *y0, *apwork;
+};
+
+template <typename XT>
+size_t filt_len(size_t n, size_t np) {
+  return (size_t)kBlk * (10 * n + 6 * (np ? np : 1));
+}
+
+template <typename XT>
+FiltBufs<XT> filt_carve(XT* base, size_t n, size_t np) {
+  FiltBufs<XT> f;
+  const size_t L = (size_t)kBlk * n, P = (size_t)kBlk * (np ? np : 1);
+  XT* p = base;
+  f.zin = carve(p, L);
+  f.yout = carve(p, L);
+  f.vk = carve(p, L);
+  f.vkm1 = carve(p, L);
+  f.vkp1 = carve(p, L);
+  f.w2 = carve(p, L);
+  f.bwork = carve(p, 4 * L);
+  f.x0 = carve(p, P);
+  f.y0 = carve(p, P);
+  f.apwork = carve(p, 4 * P);
+  return f;
+}
+
+template <typename VT, typename XT>
+void block_filter(nm_ctx* c, const Pol& pol, const GCsr<VT>& M, const GCsr<VT>& A, const GCsr<VT>& Ap,
+                  const GCsr<VT>& E, const GCsr<VT>& ET, FiltBufs<XT> f) {
+  BlockState* st = bs(c);
+  cudaStream_t s = c->stream;
+  const size_t L = (size_t)kBlk * c->n;
+  blk_init_filter<XT>(f.vk, f.vkm1, f.yout, f.zin, pol.mu[0], L, s);
+  XT *vk = f.vk, *vkm1 = f.vkm1, *vkp1 = f.vkp1;
+  for (int k = 1; k <= pol.deg; ++k) {
+    blk_mass_cheb<VT, XT>(M, c->chebB, vk, f.w2, f.bwork, s);
+    if (c->fs) {
+      blk_et<VT, XT>(ET, f.w2, f.x0, s);
+      blk_ap_cheb_persistent<VT, XT>(Ap, c->chebAp, f.x0, f.y0, f.apwork, c->bar, c->d_status, st->coop, s);
+    }
+    FiltEpi ep;
+    ep.mode = 1;
+    ep.s = (k == 1 ? 1.0 : 2.0) / pol.dd;
+    ep.cc = pol.cc;
+    ep.pm = k == 1 ? 0.0 : 1.0;
+    ep.mu = pol.mu[k];
+    blk_amv<VT, XT>(A, c->fs ? &E : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s);
+    XT* t = vkm1;
+    vkm1 = vk;
+    vk = vkp1;
+    vkp1 = t;
+  }
+}
+
+}  // namespace
+
+int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double** Uout, int* ncout, int* steps_out) {
+  BlockState* st = bs(c);
+  if (!st || !st->ok) return set_err(c, NM_ERR_ARG, "block mode needs the 3-component operator structure");
+  const int n = c->n, np = c->np, S = kBlk;
+  const bool mixed = c->precision == NM_PREC_MIXED;
+  cudaStream_t s = c->stream;
+  int rc;
+  if (!st->cublas) {
+    CB(c, cublasCreate(&st->cublas));
+    CS(c, cusolverDnCreate(&st->cusolver));
+  }
+  CB(c, cublasSetStream(st->cublas, s));
+  CS(c, cusolverDnSetStream(st->cusolver, s));
+  // ---- buffers: filter (FP32 or FP64) and FP64 Lanczos work
+  const size_t L = (size_t)S * n;
+  const size_t need32 = mixed ? filt_len<float>(n, np) : 0;
+  const size_t P = (size_t)S * (np ? np : 1);
+  const size_t need64 = (mixed ? 0 : filt_len<double>(n, np)) + 2 * L /* Wc, Vc */ + 6 * L /* B solve in, out, work */ +
+                        6 * P /* pressure block of the FP64 A-op */;
+  if (st->f32_len < need32) {
+    cudaFree(st->f32);
+    st->f32 = nullptr;
+    NM_CUDA(c, cudaMalloc(&st->f32, need32 * sizeof(float)));
+    st->f32_len = need32;
+    c->dev_bytes += need32 * 4;
+  }
+  if (st->f64_len < need64) {
+    cudaFree(st->f64);
+    st->f64 = nullptr;
+    NM_CUDA(c, cudaMalloc(&st->f64, need64 * sizeof(double)));
+    st->f64_len = need64;
+    c->dev_bytes += need64 * 8;
+  }
+  double* p64 = st->f64;
+  FiltBufs<double> f64b{};
+  if (!mixed) {
+    f64b = filt_carve<double>(p64, n, np);
+    p64 += filt_len<double>(n, np);
+  }
+  FiltBufs<float> f32b{};
+  if (mixed) f32b = filt_carve<float>(st->f32, n, np);
+  double* Wc = carve(p64, L);       // column-major n x S, ld = n
+  double* Vc = carve(p64, L);
+  double* sin_ = carve(p64, L);     // row-major block for the FP64 B solve
+  double* sout = carve(p64, L);
+  double* swork = carve(p64, 4 * L);
+  const size_t ldw = n;
+  // ---- small device matrices: S x S scratch and H (K x S), T for cuSOLVER
+  const int max_blocks = std::max(1, std::min(maxit, kMaxCols - S) / S);
+  const int Kcap = max_blocks * S + S;
+  double *dG = nullptr, *dR = nullptr, *dH = nullptr;
+  NM_CUDA(c, cudaMalloc(&dG, sizeof(double) * S * S));
+  NM_CUDA(c, cudaMalloc(&dR, sizeof(double) * S * S));
+  NM_CUDA(c, cudaMalloc(&dH, sizeof(double) * (size_t)Kcap * S));
+  auto cleanup_small = [&]() {
+    cudaFree(dG);
+    cudaFree(dR);
+    cudaFree(dH);
+  };
+  Basis& V = c->V;
+  Basis& Z = c->Z;
+  if ((rc = ensure_basis(c, V, n, S)) || (rc = ensure_basis(c, Z, n, S))) {
+    cleanup_small();
+    return rc;
+  }
+  const double one = 1.0, mone = -1.0, zero = 0.0;
+  cublasHandle_t hb = st->cublas;
+  // FP64 block B~^-1: col-major (ld ldw) in -> col-major out
+  auto bsolve_blk = [&](const double* in, size_t ldin, double* out, size_t ldout) {
+    blk_from_colmajor<double>(in, ldin, n, sin_, s);
+    blk_mass_cheb<double, double>(st->M64, c->chebB, sin_, sout, swork, s);
+    blk_to_colmajor<double>(sout, n, out, ldout, s);
+    c->n_bsolve += S;
+    c->n_spmv += c->chebB.deg;
+  };
+  auto gram = [&](const double* X, size_t ldx, const double* Y, size_t ldy, std::vector<double>& Gh) -> int {
+    CB(c, cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, S, S, n, &one, X, (int)ldx, Y, (int)ldy, &zero, dG, S));
+    Gh.resize((size_t)S * S);
+    NM_CUDA(c, cudaMemcpyAsync(Gh.data(), dG, sizeof(double) * S * S, cudaMemcpyDeviceToHost, s));
+    NM_CUDA(c, cudaStreamSynchronize(s));
+    return NM_OK;
+  };
+  // ---- start block: Z0 = deterministic vectors, V0 = B~^-1 Z0, B~^-1-orthonormalise
+  {
+    std::vector<double> h;
+    for (int j = 0; j < S; ++j) {
+      start_vector(h, n, kStartSeed + (uint64_t)j);
+      NM_CUDA(c, cudaMemcpyAsync(Z.col(j), h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+      NM_CUDA(c, cudaStreamSynchronize(s));
+    }
+  }
+  std::vector<double> Gh, Rh;
+  bsolve_blk(Z.col(0), Z.ld, V.col(0), V.ld);
+  if ((rc = gram(V.col(0), V.ld, Z.col(0), Z.ld, Gh))) return cleanup_small(), rc;
+  if (!chol_upper(Gh.data(), S, Rh)) return cleanup_small(), set_err(c, NM_ERR_NUMERIC, "start block not B-positive");
+  NM_CUDA(c, cudaMemcpyAsync(dR, Rh.data(), sizeof(double) * S * S, cudaMemcpyHostToDevice, s));
+  CB(c, cublasDtrsm(hb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, S, &one, dR, S,
+                    Z.col(0), (int)Z.ld));
+  CB(c, cublasDtrsm(hb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, S, &one, dR, S,
+                    V.col(0), (int)V.ld));
+  // ---- filter graph: zin -> yout (row-major, FP32 or FP64)
+  cudaGraphExec_t gexec = nullptr;
+  auto run_filter = [&]() {
+    if (mixed)
+      block_filter<float, float>(c, pol, st->M32, st->A32, st->Ap32, st->E32, st->ET32, f32b);
+    else
+      block_filter<double, double>(c, pol, st->M64, st->A64, st->Ap64, st->E64, st->ET64, f64b);
+  };
+  if (use_graph) {
+    cudaGraph_t g;
+    NM_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    run_filter();
+    NM_CUDA(c, cudaStreamEndCapture(s, &g));
+    NM_CUDA(c, cudaGraphInstantiate(&gexec, g, 0));
+    cudaGraphDestroy(g);
+  }
+  // ---- block tridiagonal T (host, column-major K x K built on demand)
+  std::vector<std::vector<double>> Ablk, Rblk;  // A_j (S x S), R_{j+1} (S x S)
+  double tr0 = 0.0;
+  const double eps = 2.220446049250313e-16;
+  int nblk = 0;
+  bool done = false;
+  double* dT = nullptr;
+  double* dW = nullptr;
+  double* dWork = nullptr;
+  int* dInfo = nullptr;
+  int lwork = 0;
+  NM_CUDA(c, cudaMalloc(&dInfo, sizeof(int)));
+  auto build_T = [&](int nb, std::vector<double>& T) {
+    const int K = nb * S;
+    T.assign((size_t)K * K, 0.0);
+    for (int j = 0; j < nb; ++j) {
+      for (int a = 0; a < S; ++a)
+        for (int b = 0; b < S; ++b) T[(size_t)(j * S + b) * K + j * S + a] = Ablk[j][(size_t)b * S + a];
+      if (j + 1 < nb) {
+        const std::vector<double>& R = Rblk[j];  // T(j+1, j) = R, T(j, j+1) = R^T
+        for (int a = 0; a < S; ++a)
+          for (int b = 0; b < S; ++b) {
+            T[(size_t)(j * S + b) * K + (j + 1) * S + a] = R[(size_t)b * S + a];
+            T[(size_t)((j + 1) * S + a) * K + j * S + b] = R[(size_t)b * S + a];
+          }
+      }
+    }
+  };
+  // eigen-decomposition of T on the device; vectors if want_vec
+  std::vector<double> evals;
+  auto eig_T = [&](int nb, bool want_vec) -> int {
+    const int K = nb * S;
+    std::vector<double> T;
+    build_T(nb, T);
+    cudaFree(dT);
+    cudaFree(dW);
+    dT = dW = nullptr;
+    NM_CUDA(c, cudaMalloc(&dT, sizeof(double) * (size_t)K * K));
+    NM_CUDA(c, cudaMalloc(&dW, sizeof(double) * K));
+    NM_CUDA(c, cudaMemcpyAsync(dT, T.data(), sizeof(double) * (size_t)K * K, cudaMemcpyHostToDevice, s));
+    const cusolverEigMode_t jobz = want_vec ? CUSOLVER_EIG_MODE_VECTOR : CUSOLVER_EIG_MODE_NOVECTOR;
+    int lw = 0;
+    CS(c, cusolverDnDsyevd_bufferSize(st->cusolver, jobz, CUBLAS_FILL_MODE_LOWER, K, dT, K, dW, &lw));
+    if (lw > lwork) {
+      cudaFree(dWork);
+      NM_CUDA(c, cudaMalloc(&dWork, sizeof(double) * lw));
+      lwork = lw;
+    }
+    CS(c, cusolverDnDsyevd(st->cusolver, jobz, CUBLAS_FILL_MODE_LOWER, K, dT, K, dW, dWork, lwork, dInfo));
+    evals.resize(K);
+    int info = 0;
+    NM_CUDA(c, cudaMemcpyAsync(evals.data(), dW, sizeof(double) * K, cudaMemcpyDeviceToHost, s));
+    NM_CUDA(c, cudaMemcpyAsync(&info, dInfo, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NM_CUDA(c, cudaStreamSynchronize(s));
+    if (info != 0) return set_err(c, NM_ERR_NUMERIC, "dense eigensolve of T failed");
+    return NM_OK;
+  };
+  auto fail = [&](int code) {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    cleanup_small();
+    cudaFree(dT);
+    cudaFree(dW);
+    cudaFree(dWork);
+    cudaFree(dInfo);
+    return code;
+  };
+  for (int j = 0; j < max_blocks; ++j) {
+    const int K = (j + 1) * S;  // basis columns 0..K-1 hold blocks 0..j
+    // W = F(Z_j)
+    if (mixed) blk_gather_cols<float>(Z, j * S, n, f32b.zin, s);
+    else blk_gather_cols<double>(Z, j * S, n, f64b.zin, s);
+    if (gexec) NM_CUDA(c, cudaGraphLaunch(gexec, s));
+    else run_filter();
+    c->n_amv += (long long)pol.deg * S;
+    c->n_bsolve += (long long)pol.deg * S;
+    c->n_spmv += (long long)pol.deg * (c->chebB.deg + (c->fs ? 2 + c->chebAp.deg : 1));
+    if (mixed) blk_to_colmajor<float>(f32b.yout, n, Wc, ldw, s);
+    else blk_to_colmajor<double>(f64b.yout, n, Wc, ldw, s);
+    // W -= Z_{j-1} R_j^T
+    if (j > 0) {
+      NM_CUDA(c, cudaMemcpyAsync(dR, Rblk[j - 1].data(), sizeof(double) * S * S, cudaMemcpyHostToDevice, s));
+      CB(c, cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_T, n, S, S, &mone, Z.col((j - 1) * S), (int)Z.ld, dR, S, &one, Wc,
+                        (int)ldw));
+    }
+    // A_j = V_j^T W (symmetrised), W -= Z_j A_j
+    if ((rc = gram(V.col(j * S), V.ld, Wc, ldw, Gh))) return fail(rc);
+    std::vector<double> Aj((size_t)S * S);
+    for (int a = 0; a < S; ++a)
+      for (int b = 0; b < S; ++b) Aj[(size_t)b * S + a] = 0.5 * (Gh[(size_t)b * S + a] + Gh[(size_t)a * S + b]);
+    for (double x : Aj)
+      if (!std::isfinite(x)) return fail(set_err(c, NM_ERR_NUMERIC, "non-finite block Lanczos coefficient"));
+    Ablk.push_back(Aj);
+    NM_CUDA(c, cudaMemcpyAsync(dG, Aj.data(), sizeof(double) * S * S, cudaMemcpyHostToDevice, s));
+    CB(c, cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, S, S, &mone, Z.col(j * S), (int)Z.ld, dG, S, &one, Wc, (int)ldw));
+    // full block Gram-Schmidt, two classical passes: H = V^T W, W -= Z H
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int c0 = 0; c0 < K; c0 += Basis::kChunk) {
+        const int w = std::min(Basis::kChunk, K - c0);
+        CB(c, cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, w, S, n, &one, V.col(c0), (int)V.ld, Wc, (int)ldw, &zero,
+                          dH + c0, Kcap));
+      }
+      for (int c0 = 0; c0 < K; c0 += Basis::kChunk) {
+        const int w = std::min(Basis::kChunk, K - c0);
+        CB(c, cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, S, w, &mone, Z.col(c0), (int)Z.ld, dH + c0, Kcap, &one, Wc,
+                          (int)ldw));
+      }
+    }
+    // Vn = B~^-1 W;  R from the Cholesky of Vn^T W;  Z_{j+1} = W R^-1, V_{j+1} = Vn R^-1
+    bsolve_blk(Wc, ldw, Vc, ldw);
+    if ((rc = gram(Vc, ldw, Wc, ldw, Gh))) return fail(rc);
+    nblk = j + 1;
+    if (!chol_upper(Gh.data(), S, Rh)) {
+      done = true;  // block breakdown: the Krylov space is exhausted
+      break;
+    }
+    Rblk.push_back(Rh);
+    if ((rc = ensure_basis(c, V, n, K + S)) || (rc = ensure_basis(c, Z, n, K + S))) return fail(rc);
+    NM_CUDA(c, cudaMemcpyAsync(dR, Rh.data(), sizeof(double) * S * S, cudaMemcpyHostToDevice, s));
+    NM_CUDA(c, cudaMemcpy2DAsync(Z.col(K), Z.ld * sizeof(double), Wc, ldw * sizeof(double), n * sizeof(double), S,
+                                 cudaMemcpyDeviceToDevice, s));
+    NM_CUDA(c, cudaMemcpy2DAsync(V.col(K), V.ld * sizeof(double), Vc, ldw * sizeof(double), n * sizeof(double), S,
+                                 cudaMemcpyDeviceToDevice, s));
+    CB(c, cublasDtrsm(hb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, S, &one, dR,
+                      S, Z.col(K), (int)Z.ld));
+    CB(c, cublasDtrsm(hb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, S, &one, dR,
+                      S, V.col(K), (int)V.ld));
+    // restricted-trace convergence test every 64 vectors, first after eight
+    // block steps: a block Krylov space of degree < 8 has not yet lifted the
+    // wanted Ritz values above the bar, so an empty Ritz set that early would
+    // end the solve through the "no eigenvalue in the interval" exit.
+    if (K < 50 || j < 7 || ((K / S) % 2) != 0) continue;
+    if ((rc = eig_T(nblk, false))) return fail(rc);
+    double tr1 = 0.0;
+    int cnt = 0;
+    for (double x : evals)
+      if (x + eps >= pol.bar) {
+        tr1 += x;
+        ++cnt;
+      }
+    if (c->verbose) printf(" block %4d (K %5d): nconv %4d  tr1 %21.15e\n", j, K, cnt, tr1);
+    if (std::fabs(tr1 - tr0) < 2e-12 || std::fabs(tr1) + std::fabs(tr0) < 1e-10) {
+      done = true;
+      break;
+    }
+    tr0 = tr1;
+  }
+  (void)done;
+  if (gexec) {
+    cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+  }
+  // ---- Ritz vectors for eigenvalues of T above the bar
+  const int K = nblk * S;
+  if ((rc = eig_T(nblk, true))) return fail(rc);
+  int first = K;
+  for (int i = 0; i < K; ++i)
+    if (evals[i] >= pol.bar) {
+      first = i;
+      break;
+    }
+  const int nc = K - first;
+  double* U = nullptr;
+  if (nc > 0) {
+    NM_CUDA(c, cudaMalloc(&U, sizeof(double) * (size_t)n * nc));
+    const double* Ssel = dT + (size_t)first * K;  // eigenvectors first..K-1, ld = K
+    for (int c0 = 0; c0 < K; c0 += Basis::kChunk) {
+      const int w = std::min(Basis::kChunk, K - c0);
+      const double beta = c0 == 0 ? 0.0 : 1.0;
+      CB(c, cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, nc, w, &one, V.col(c0), (int)V.ld, Ssel + c0, K, &beta, U, n));
+    }
+  }
+  NM_CUDA(c, cudaStreamSynchronize(s));
+  fail(NM_OK);  // releases the scratch (T, workspace, small matrices)
+  *Uout = U;
+  *ncout = nc;
+  *steps_out = K;
+  return NM_OK;
+}
+
+int rayleigh_ritz64(nm_ctx* c, double** Uio, int nc) {
+  BlockState* st = bs(c);
+  if (!st || !st->ok || !st->cublas || nc <= 0) return NM_OK;
+  const int n = c->n, np = c->np, S = kBlk;
+  const int ncp = (nc + S - 1) / S * S;  // zero-padded to whole 32-column blocks
+  cudaStream_t s = c->stream;
+  const size_t L = (size_t)S * n, P = (size_t)S * (np ? np : 1);
+  const bool mixed = c->precision == NM_PREC_MIXED;
+  double* p64 = st->f64 + (mixed ? 0 : filt_len<double>(n, np)) + 2 * L;
+  double* sin_ = carve(p64, L);
+  double* sout = carve(p64, L);
+  carve(p64, 4 * L);
+  double* x0 = carve(p64, P);
+  double* y0 = carve(p64, P);
+  double* apw = carve(p64, 4 * P);
+  double* U = *Uio;
+  double *Up = nullptr, *AU = nullptr, *BU = nullptr, *GA = nullptr, *GB = nullptr, *W = nullptr, *work = nullptr;
+  int* info = nullptr;
+  auto release = [&]() {
+    cudaFree(Up);
+    cudaFree(AU);
+    cudaFree(BU);
+    cudaFree(GA);
+    cudaFree(GB);
+    cudaFree(W);
+    cudaFree(work);
+    cudaFree(info);
+  };
+  const size_t nb = sizeof(double) * (size_t)n * ncp;
+  if (cudaMalloc(&Up, nb) != cudaSuccess || cudaMalloc(&AU, nb) != cudaSuccess || cudaMalloc(&BU, nb) != cudaSuccess ||
+      cudaMalloc(&GA, sizeof(double) * (size_t)nc * nc) != cudaSuccess ||
+      cudaMalloc(&GB, sizeof(double) * (size_t)nc * nc) != cudaSuccess ||
+      cudaMalloc(&W, sizeof(double) * nc) != cudaSuccess || cudaMalloc(&info, sizeof(int)) != cudaSuccess) {
+    release();
+    return set_err(c, NM_ERR_OOM, "Rayleigh-Ritz workspace");
+  }
+  NM_CUDA(c, cudaMemsetAsync(Up, 0, nb, s));
+  NM_CUDA(c, cudaMemcpyAsync(Up, U, sizeof(double) * (size_t)n * nc, cudaMemcpyDeviceToDevice, s));
+  FiltEpi ep;  // mode 0: plain product
+  for (int j0 = 0; j0 < ncp; j0 += S) {
+    blk_from_colmajor<double>(Up + (size_t)j0 * n, n, n, sin_, s);
+    if (c->fs) {
+      blk_et<double, double>(st->ET64, sin_, x0, s);
+      blk_ap_cheb_persistent<double, double>(st->Ap64, c->chebAp, x0, y0, apw, c->bar, c->d_status, st->coop, s);
+    }
+    blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sout, nullptr, nullptr, nullptr, ep, s);
+    blk_to_colmajor<double>(sout, n, AU + (size_t)j0 * n, n, s);
+    blk_mass_spmv<double>(st->M64, sin_, sout, s);
+    blk_to_colmajor<double>(sout, n, BU + (size_t)j0 * n, n, s);
+  }
+  c->n_amv += ncp;
+  c->n_spmv += (long long)(ncp / S) * (c->fs ? 3 + c->chebAp.deg : 2);
+  const double one = 1.0, zero = 0.0;
+  CB(c, cublasDgemm(st->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nc, nc, n, &one, Up, n, AU, n, &zero, GA, nc));
+  CB(c, cublasDgemm(st->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nc, nc, n, &one, Up, n, BU, n, &zero, GB, nc));
+  int lw = 0;
+  CS(c, cusolverDnDsygvd_bufferSize(st->cusolver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+                                    CUBLAS_FILL_MODE_LOWER, nc, GA, nc, GB, nc, W, &lw));
+  NM_CUDA(c, cudaMalloc(&work, sizeof(double) * std::max(lw, 1)));
+  CS(c, cusolverDnDsygvd(st->cusolver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, nc, GA,
+                         nc, GB, nc, W, work, lw, info));
+  int hinfo = 0;
+  NM_CUDA(c, cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NM_CUDA(c, cudaStreamSynchronize(s));
+  if (hinfo != 0) {
+    release();
+    return set_err(c, NM_ERR_NUMERIC, "Rayleigh-Ritz generalized eigensolve failed");
+  }
+  // U <- U Q  (Q in GA, B-orthonormal columns)
+  CB(c, cublasDgemm(st->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, nc, nc, &one, Up, n, GA, nc, &zero, U, n));
+  NM_CUDA(c, cudaStreamSynchronize(s));
+  release();
+  return NM_OK;
+}
+
+}  // namespace nmg

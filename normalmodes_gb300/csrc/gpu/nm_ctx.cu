@@ -13,6 +13,7 @@
 #include <cstring>
 #include <vector>
 
+#include "nm_block.h"
 #include "nm_internal.h"
 #include "nm_ops.h"
 
@@ -209,6 +210,7 @@ int nm_create(nm_ctx** out, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, 
     cudaMemcpy(c->Dp, c->hDp.data(), sizeof(double) * c->np, cudaMemcpyHostToDevice);
   }
   if ((rc = alloc_work(c))) return bail(rc);
+  if ((rc = block_build(c, A, B, Ap, E, ET))) return bail(rc);
   // Bounds and Chebyshev set-ups.
   c->chebB.deg = o.b_cheb_deg > 0 ? o.b_cheb_deg : (c->porder == 2 ? 45 : 25);
   if (o.b_bounds[1] > 0) {
@@ -248,6 +250,7 @@ void nm_destroy(nm_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_basis(c->V);
   free_basis(c->Z);
+  block_free(c);
   for (auto* m : {&c->A, &c->B, &c->Ap, &c->E, &c->ET}) free_sell(*m);
   for (auto* m : {&c->A32, &c->B32, &c->Ap32, &c->E32, &c->ET32}) free_sell(*m);
   for (int i = 0; i < 16; ++i)

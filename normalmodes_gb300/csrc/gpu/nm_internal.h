@@ -110,6 +110,9 @@ struct nm_ctx {
   size_t dev_bytes = 0;
   long long n_amv = 0, n_bsolve = 0, n_spmv = 0;
   nmg::Basis V, Z;
+  // block (batched) path: grouped operators and buffers, built on first use
+  void* blk = nullptr;  // nmg::BlockState*
+  const nm_csr* src[5] = {nullptr};  // not owned; only valid inside nm_create
 };
 
 namespace nmg {

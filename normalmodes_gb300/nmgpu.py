@@ -47,7 +47,7 @@ class NmOpts(C.Structure):
 class NmSolveOpts(C.Structure):
     _fields_ = [("maxit", C.c_int), ("tol", C.c_double), ("thresh_int", C.c_double), ("thresh_ext", C.c_double),
                 ("mlan_bounds", C.c_int), ("ab_bounds", C.c_double * 2), ("damping", C.c_int),
-                ("want_vectors", C.c_int), ("unscale", C.c_int), ("use_graph", C.c_int)]
+                ("want_vectors", C.c_int), ("unscale", C.c_int), ("use_graph", C.c_int), ("block", C.c_int)]
 
 
 class NmResult(C.Structure):
@@ -227,7 +227,7 @@ class Solver:
 
     def solve(self, lowfreq: float, upfreq: float, maxit: int = 0, tol: float = 0.0, ab_bounds=None,
               want_vectors: bool = True, unscale: bool = False, use_graph: bool = True, damping: int = 1,
-              mlan_bounds: int = 0, allow_noconv: bool = False) -> SolveResult:
+              mlan_bounds: int = 0, allow_noconv: bool = False, block: int = 0) -> SolveResult:
         L = lib()
         o = NmSolveOpts()
         L.nm_default_solve_opts(C.byref(o))
@@ -238,6 +238,7 @@ class Solver:
         o.use_graph = int(use_graph)
         o.damping = damping
         o.mlan_bounds = mlan_bounds
+        o.block = block
         if ab_bounds is not None:
             o.ab_bounds[0], o.ab_bounds[1] = ab_bounds
         r = NmResult()
