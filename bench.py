@@ -1,0 +1,361 @@
+#!/usr/bin/env python3
+"""Benchmark of the NormalModes eigensolve on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision mixed|fp64] [--block 32|0] [--config 1|0]
+
+Workload (configs[1] of the benchmark definition): the seeded 3-layer ball
+(inner core solid, fluid outer core, solid mantle; 36^3 * 6 = 279,936 P2
+tetrahedra, 1,198,455 displacement DOFs + 67,590 pressure DOFs, ~83 nnz per
+row of Ad), all eigenpairs in 0.1-2.0 mHz.  A step is one complete
+polynomial-filtered Lanczos solve of that interval (bounds, filter design,
+filtered Lanczos, Ritz vectors, residual check) with the operators already
+resident in HBM; value = eigenpairs found / time (all ranks).  Every
+operator is larger than L2 (Ad alone is 1.2 GB), so no L2 flush is needed.
+
+`e2e` repeats the step through the C-ABI with host buffers: nm_create from
+pinned host CSR arrays (H2D inside the timed region), nm_solve, eigenvalues
+and eigenvectors back to host (D2H), nm_destroy.
+
+`--impl reference` times the CPU path (the FP64 C/OpenMP restatement under
+oracle/, since the Fortran/MPI/pEVSL reference cannot be built here) on a
+bounded sample of the same workload and projects eigenpairs/s; it never
+touches the GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "eigenpairs/s at resid<=1e-10: mixed+batched vs plain FP64 on GB300; SpMV HBM GB/s"
+CONFIGS = {
+    1: dict(name="configs[1]: layered ball, 279,936 P2 tets, 1.2M DOF, 0.1-2.0 mHz",
+            model=dict(n_cells=36, porder=2), porder=2, interval=(0.1, 2.0)),
+    0: dict(name="configs[0]: layered ball, 10,368 P1 tets, 0.2-1.0 mHz",
+            model=dict(n_cells=12, porder=1), porder=1, interval=(0.2, 1.0)),
+}
+# Reference-algorithm step counts of configs[1] measured on GB300 with the
+# single-vector ChebLanNr (used only to scale the CPU samples).
+REF_COUNTS = {1: dict(nev=1232, lanczos_steps=4401, degree=125), 0: None}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--block", type=int, default=32)
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------- distributed
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce(x: float, ws: int, op: str) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------- clocks
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile(prefix="clk", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+        self.f.close()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.f.name):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        finally:
+            try:
+                os.unlink(self.f.name)
+            except OSError:
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch(key: str):
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        v = d.get(key)
+        if v is not None:
+            return float(v)
+    return None
+
+
+# ----------------------------------------------------------------------------- CPU sample
+def cpu_sample(cfg_id: int, mats, porder: int, seconds: float, bounds=None):
+    """Time filter degree steps of the FP64 CPU restatement (all host threads)
+    and project the reference algorithm's eigenpairs/s for the workload."""
+    from oracle import oracle as O
+    import numpy as np
+    t0 = time.perf_counter()
+    op = O.setup_operator(mats, porder, bounds=bounds)
+    t_setup = time.perf_counter() - t0
+    refc = REF_COUNTS.get(cfg_id)
+    if refc is None:
+        # small configuration: the whole reference solve runs on the CPU
+        t1 = time.perf_counter()
+        r = O.apply_pevsl(op, *CONFIGS[cfg_id]["interval"])
+        t_solve = time.perf_counter() - t1
+        op.close()
+        return {"value": len(r.lam) / t_solve, "unit": "eigenpairs/s", "cores": os.cpu_count(), "kind": "port",
+                "sample": f"complete FP64 C/OpenMP solve: {len(r.lam)} eigenpairs in {t_solve:.1f} s",
+                "t_setup_s": t_setup}
+    # one degree step of the filter = one B~^-1 apply + one A-op + recurrence
+    pol = O.Pol(deg=1, mu=np.array([0.0, 1.0]), cc=0.0, dd=1.0, gam=0.0, bar=0.0, kind="interior")
+    v = O.start_vector(op.n)
+    op.chebav(pol, v)  # warm
+    steps, t = 0, 0.0
+    while t < seconds and steps < 64:
+        t1 = time.perf_counter()
+        op.chebav(pol, v)
+        t += time.perf_counter() - t1
+        steps += 1
+    t_deg = t / steps
+    if refc:
+        t_solve = refc["lanczos_steps"] * refc["degree"] * t_deg
+        value = refc["nev"] / t_solve
+        sample = (f"{steps} filter degree steps (B~^-1 Chebyshev solve of degree {op.b_cheb[2]} + A-op with "
+                  f"Ap Chebyshev of degree {op.ap_cheb[2] if op.ap_cheb else 0}) of the FP64 C/OpenMP restatement "
+                  f"on the full workload, {t_deg:.3f} s each; eigenpairs/s = {refc['nev']} / "
+                  f"({refc['lanczos_steps']} Lanczos steps x degree {refc['degree']} x step time)")
+    else:
+        value, sample = None, f"{steps} filter degree steps, {t_deg:.3f} s each"
+    op.close()
+    return {"value": value, "unit": "eigenpairs/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": sample, "t_degree_step_s": t_deg, "t_setup_s": t_setup}
+
+
+# ----------------------------------------------------------------------------- main
+def main():
+    a = parse()
+    ws, rank, local = dist_init()
+    cfg = CONFIGS[a.config]
+    lo, hi = cfg["interval"]
+    from normalmodes_gb300.model import Model
+    mdl = Model.ball(**cfg["model"])
+    mats = mdl.operators()
+    info = mdl.info()
+
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        b = cpu_sample(a.config, mats, cfg["porder"], a.cpu_seconds)
+        for _ in range(a.warmup):
+            pass  # each step is a bounded CPU sample; warm-up is inside cpu_sample
+        vals = [b["value"]]
+        for _ in range(max(0, a.steps - 1)):
+            vals.append(cpu_sample(a.config, mats, cfg["porder"], a.cpu_seconds)["value"])
+        v = statistics.mean(vals) if vals[0] is not None else None
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "eigenpairs/s", "n_gpus": a.gpus,
+                "steps": a.steps, "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": cfg["name"], "n_dof": info.n, "n_pressure": info.np},
+                "cpu_baseline": {**b, "value": v},
+                "e2e": {"value": v, "unit": "eigenpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    from normalmodes_gb300 import nmgpu
+    from normalmodes_gb300.nmgpu import Solver, NM_PREC_MIXED, NM_PREC_FP64
+    prec = NM_PREC_MIXED if a.precision == "mixed" else NM_PREC_FP64
+    dev = local
+    torch.cuda.set_device(dev)
+    sv = Solver(mats, cfg["porder"], device=dev, precision=prec)
+    sinfo = sv.info()
+    stream = torch.cuda.ExternalStream(sv.stream)
+
+    def solve(s, want_vectors=False):
+        return s.solve(lo, hi, block=a.block, want_vectors=want_vectors)
+
+    for _ in range(a.warmup):
+        solve(sv)
+    barrier(ws)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    nev_tot, kernels, res = 0, 0, None
+    with Clocks(dev) as clk:
+        ev0.record(stream)
+        for _ in range(a.steps):
+            res = solve(sv)
+            nev_tot += len(res.lam)
+            kernels += res.counts["kernels"]
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier(ws)
+    t_local = ev0.elapsed_time(ev1) / 1e3
+    t = allreduce(t_local, ws, "max")
+    nev_all = allreduce(float(nev_tot), ws, "sum")
+    value = nev_all / t
+    clocks = clk.summary()
+
+    # roofline of the dominant kernel (block mass Chebyshev step)
+    which = 4 if a.block > 1 else 2
+    ms, by, la = sv.time_op(which, 10)
+    per_launch_ms = ms / la
+    achieved = (by / la) / (per_launch_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    roof = {"kernel": "k_mass_cheb (block 32, " + ("fp32" if prec == NM_PREC_MIXED else "fp64") + ")"
+            if a.block > 1 else "k_cheb (fp64 SELL)",
+            "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "algorithmic_bytes_per_launch": by / la,
+            "launch_ms": per_launch_ms,
+            "traffic": traffic_per_launch("k_mass_cheb_block32_fp32" if a.block > 1 and prec == NM_PREC_MIXED
+                                          else "k_mass_cheb_block32_fp64" if a.block > 1 else "k_cheb_fp64")}
+    spmv = {}
+    ms_b, by_b, _ = sv.time_op(1, 20)
+    spmv["fp64_sell_B_spmv_GBs"] = round(by_b / ms_b / 1e6, 1)
+    ms_f, by_f, la_f = sv.time_op(6 if a.block > 1 else 3, 3)
+    spmv["filter_degree_step_ms"] = round(ms_f, 3)
+    spmv["filter_degree_step_GBs"] = round(by_f / ms_f / 1e6, 1)
+
+    # end to end through the C-ABI with host buffers
+    e2e = None
+    if not a.no_e2e:
+        import numpy as np
+        pinned = {}
+        for k, m in mats.items():
+            pinned[k] = type(m)(torch.from_numpy(m.rowptr).pin_memory().numpy(),
+                                torch.from_numpy(m.col).pin_memory().numpy(),
+                                torch.from_numpy(m.val).pin_memory().numpy(), m.shape)
+        barrier(ws)
+        torch.cuda.synchronize()
+        te0 = time.perf_counter()
+        nev_e, h2d, d2h = 0, 0, 0
+        for _ in range(a.steps):
+            s2 = Solver(pinned, cfg["porder"], device=dev, precision=prec)
+            h2d += s2.info().h2d_bytes
+            r2 = s2.solve(lo, hi, block=a.block, want_vectors=True)
+            nev_e += len(r2.lam)
+            d2h += 8 * (r2.vec.size + 3 * len(r2.lam)) if r2.vec is not None else 8 * 3 * len(r2.lam)
+            s2.close()
+        torch.cuda.synchronize()
+        te = allreduce(time.perf_counter() - te0, ws, "max")
+        e2e = {"value": allreduce(float(nev_e), ws, "sum") / te, "unit": "eigenpairs/s",
+               "h2d_bytes_per_step": h2d // a.steps, "d2h_bytes_per_step": d2h // a.steps}
+
+    cpu = None
+    if rank == 0 and not a.no_cpu:
+        cpu = cpu_sample(a.config, mats, cfg["porder"], a.cpu_seconds,
+                         bounds={"B": tuple(sinfo.b_bounds), "Ap": tuple(sinfo.ap_bounds)} if sinfo.fs else
+                         {"B": tuple(sinfo.b_bounds)})
+    if rank != 0:
+        sv.close()
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "eigenpairs/s", "n_gpus": ws, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": t * 1e3 / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 filter SpMM / f64 Lanczos, Gram-Schmidt, Rayleigh-Ritz" if prec == NM_PREC_MIXED else "f64",
+        "data": "synthetic",
+        "config": {"workload": cfg["name"], "n_dof": info.n, "n_pressure": info.np, "nnz": list(info.nnz),
+                   "interval_mhz": [lo, hi], "precision": a.precision, "block": a.block,
+                   "l2": "operators and vectors exceed L2 (Ad 1.2 GB); no flush",
+                   "eigenpairs_per_step": len(res.lam), "lanczos_vectors": res.lanczos_steps,
+                   "filter_degree": res.pol_deg, "max_err_ref": float(res.err_ref.max()) if len(res.lam) else None,
+                   "max_res2": float(res.res2.max()) if len(res.lam) else None,
+                   "parallelism": f"replicas x{ws}"},
+        "gpu_launches": kernels,
+        "clocks": clocks,
+        "roofline": roof,
+        "spmv": spmv,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "times_s": res.times,
+    }
+    print(json.dumps(line))
+    sv.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -94,6 +94,7 @@ typedef struct {
   int nritz_above_bar;
   double t_bounds, t_filter_design, t_lanczos, t_ritz, t_total; /* seconds        */
   long long n_amv, n_bsolve, n_spmv; /* operator applications / SpMV launches       */
+  long long n_kernels;   /* kernels of this library launched by the solve            */
 } nm_result;
 
 typedef struct nm_ctx nm_ctx;
@@ -146,7 +147,9 @@ int nm_sync(nm_ctx* ctx);
  * applications of the selected operator on device vectors and returns the
  * mean time per application in milliseconds and the algorithmic bytes one
  * application moves.  which: 0 = A-op, 1 = B SpMV, 2 = B Chebyshev solve,
- * 3 = one filter degree step (B-solve + A-op + recurrence). */
+ * 3 = one filter degree step (B-solve + A-op + recurrence); block (32-column,
+ * in the context's precision): 4 = mass Chebyshev solve, 5 = A-op, 6 = one
+ * filter degree step. */
 int nm_time_op(nm_ctx* ctx, int which, int reps, double* ms_per_op, double* bytes_per_op, int* launches_per_op);
 
 #ifdef __cplusplus

@@ -485,17 +485,20 @@ void blk_mass_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, X
     else if (last) NM_MC(false, true);
     else NM_MC(false, false);
 #undef NM_MC
+    nmg::add_launches(1);
   }
 }
 
 template <typename VT>
 void blk_mass_spmv(const GCsr<VT>& M, const double* x, double* y, cudaStream_t s) {
   k_mass_spmv<VT><<<nrb(M.nrows), kT, 0, s>>>(M.nrows, M.rp, M.ci, M.v, x, y);
+  nmg::add_launches(1);
 }
 
 template <typename VT, typename XT>
 void blk_et(const GCsr<VT>& ET, const XT* w, XT* x0, cudaStream_t s) {
   k_et<VT, XT><<<nrb(ET.nrows), kT, 0, s>>>(ET.nrows, ET.rp, ET.ci, ET.v, w, x0);
+  nmg::add_launches(1);
 }
 
 template <typename VT, typename XT>
@@ -523,6 +526,7 @@ void blk_ap_cheb_persistent(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b
   int deg = ch.deg;
   cudaLaunchKernelEx(&cfg, k_ap_cheb<VT, XT>, np, (const int*)Ap.rp, (const int*)Ap.ci, (const VT*)Ap.v, b, x, r, xi,
                      d0, d1, (const double*)ch.d_coef, deg, it, bar, status);
+  nmg::add_launches(1);
 }
 
 int blk_coop_blocks() {
@@ -555,19 +559,23 @@ void blk_amv(const GCsr<VT>& A, const GCsr<VT>* E, const XT* v, const XT* y, XT*
     else NM_AMV(false, 1);
   }
 #undef NM_AMV
+  nmg::add_launches(1);
 }
 
 template <typename XT>
 void blk_gather_cols(const Basis& Z, int j0, int n, XT* blk, cudaStream_t s) {
   k_gather_cols<XT><<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(Z.d_chunks, Z.ld, j0, n, blk);
+  nmg::add_launches(1);
 }
 template <typename XT>
 void blk_to_colmajor(const XT* blk, int n, double* out, size_t ld, cudaStream_t s) {
   k_to_colmajor<XT><<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(blk, n, out, ld);
+  nmg::add_launches(1);
 }
 template <typename XT>
 void blk_from_colmajor(const double* src, size_t ld, int n, XT* blk, cudaStream_t s) {
   k_from_colmajor<XT><<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(src, ld, n, blk);
+  nmg::add_launches(1);
 }
 template void blk_from_colmajor<float>(const double*, size_t, int, float*, cudaStream_t);
 template void blk_from_colmajor<double>(const double*, size_t, int, double*, cudaStream_t);
@@ -575,6 +583,7 @@ template void blk_from_colmajor<double>(const double*, size_t, int, double*, cud
 template <typename XT>
 void blk_init_filter(XT* vk, XT* vkm1, XT* y, const XT* v, double mu0, size_t len, cudaStream_t s) {
   k_init_filter_blk<XT><<<(int)((len + 255) / 256), 256, 0, s>>>(vk, vkm1, y, v, (XT)mu0, len);
+  nmg::add_launches(1);
 }
 
 #define NM_INST(VT, XT)                                                                                              \

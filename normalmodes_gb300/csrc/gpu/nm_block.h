@@ -86,6 +86,8 @@ struct BlockState {
   cusolverDnHandle_t cusolver = nullptr;
   int coop = 0;
 };
+int block_buffers(nm_ctx* c);
+int block_time_op(nm_ctx* c, int which, int reps, double* ms, double* bytes, int* launches_per_op);
 int block_build(nm_ctx* c, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, const nm_csr* E, const nm_csr* ET);
 void block_free(nm_ctx* c);
 // Block filtered Lanczos; on success U (n x nc, column-major, device, owned

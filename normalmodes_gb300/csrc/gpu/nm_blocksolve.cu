@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <vector>
 
 #include "nm_block.h"
@@ -160,25 +161,22 @@ void block_filter(nm_ctx* c, const Pol& pol, const GCsr<VT>& M, const GCsr<VT>& 
 
 }  // namespace
 
-int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double** Uout, int* ncout, int* steps_out) {
+int block_buffers(nm_ctx* c) {
   BlockState* st = bs(c);
   if (!st || !st->ok) return set_err(c, NM_ERR_ARG, "block mode needs the 3-component operator structure");
   const int n = c->n, np = c->np, S = kBlk;
   const bool mixed = c->precision == NM_PREC_MIXED;
-  cudaStream_t s = c->stream;
-  int rc;
   if (!st->cublas) {
     CB(c, cublasCreate(&st->cublas));
     CS(c, cusolverDnCreate(&st->cusolver));
   }
-  CB(c, cublasSetStream(st->cublas, s));
-  CS(c, cusolverDnSetStream(st->cusolver, s));
-  // ---- buffers: filter (FP32 or FP64) and FP64 Lanczos work
+  CB(c, cublasSetStream(st->cublas, c->stream));
+  CS(c, cusolverDnSetStream(st->cusolver, c->stream));
   const size_t L = (size_t)S * n;
-  const size_t need32 = mixed ? filt_len<float>(n, np) : 0;
   const size_t P = (size_t)S * (np ? np : 1);
   const size_t need64 = (mixed ? 0 : filt_len<double>(n, np)) + 2 * L /* Wc, Vc */ + 6 * L /* B solve in, out, work */ +
                         6 * P /* pressure block of the FP64 A-op */;
+  const size_t need32 = mixed ? filt_len<float>(n, np) : 0;
   if (st->f32_len < need32) {
     cudaFree(st->f32);
     st->f32 = nullptr;
@@ -193,6 +191,112 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
     st->f64_len = need64;
     c->dev_bytes += need64 * 8;
   }
+  return NM_OK;
+}
+
+// Timing of the block operators (CUDA events on the context's stream).
+// which 4: block mass Chebyshev solve; 5: block A-op; 6: one block filter
+// degree step.  Bytes are algorithmic: each matrix once, each vector stream
+// once per kernel.
+int block_time_op(nm_ctx* c, int which, int reps, double* ms, double* bytes, int* launches_per_op) {
+  int rc;
+  if ((rc = block_buffers(c))) return rc;
+  BlockState* st = bs(c);
+  const int n = c->n, np = c->np, S = kBlk;
+  const bool mixed = c->precision == NM_PREC_MIXED;
+  const size_t xs = mixed ? 4 : 8, vs = mixed ? 4 : 8;
+  const double L = (double)S * n, P = (double)S * np;
+  const long long nnzM = mixed ? st->M32.nnz : st->M64.nnz;
+  const long long nnzA = mixed ? st->A32.nnz : st->A64.nnz;
+  const long long nnzE = c->fs ? (mixed ? st->E32.nnz : st->E64.nnz) : 0;
+  const long long nnzET = c->fs ? (mixed ? st->ET32.nnz : st->ET64.nnz) : 0;
+  const long long nnzAp = c->fs ? (mixed ? st->Ap32.nnz : st->Ap64.nnz) : 0;
+  const int dB = c->chebB.deg, dAp = c->chebAp.deg;
+  // per Chebyshev step on the mass: matrix + row pointers + 6 vector streams
+  const double b_iter = (double)nnzM * (vs + 4) + (double)(n / 3 + 1) * 4 + 6.0 * L * xs;
+  const double ap_iter = c->fs ? (double)nnzAp * (vs + 4) + (double)(np + 1) * 4 + 6.0 * P * xs : 0.0;
+  const double et = c->fs ? (double)nnzET * (3 * vs + 4) + (double)(np + 1) * 4 + L * xs + P * xs : 0.0;
+  const double amv = (double)nnzA * (9 * vs + 4) + (double)(n / 3 + 1) * 4 + (double)nnzE * (3 * vs + 4) +
+                     L * xs /* v */ + (c->fs ? P * xs : 0.0) + 4.0 * L * xs /* vk, vkm1, out, yacc */;
+  double by = 0;
+  int la = 0;
+  std::function<void()> run;
+  FiltEpi ep;
+  ep.mode = 1;
+  ep.s = 2.0;
+  ep.cc = 0.0;
+  ep.pm = 1.0;
+  ep.mu = 0.1;
+  const bool wantB = which == 4 || which == 6, wantA = which == 5 || which == 6;
+  if (mixed) {
+    FiltBufs<float> f = filt_carve<float>(st->f32, n, np);
+    NM_CUDA(c, cudaMemsetAsync(st->f32, 0, sizeof(float) * st->f32_len, c->stream));
+    run = [=]() {
+      if (wantB) blk_mass_cheb<float, float>(st->M32, c->chebB, f.vk, f.w2, f.bwork, c->stream);
+      if (wantA) {
+        if (c->fs) {
+          blk_et<float, float>(st->ET32, f.w2, f.x0, c->stream);
+          blk_ap_cheb_persistent<float, float>(st->Ap32, c->chebAp, f.x0, f.y0, f.apwork, c->bar, c->d_status,
+                                               st->coop, c->stream);
+        }
+        blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, f.vkp1, f.vk, f.vkm1, f.yout, ep,
+                              c->stream);
+      }
+    };
+  } else {
+    FiltBufs<double> f = filt_carve<double>(st->f64, n, np);
+    NM_CUDA(c, cudaMemsetAsync(st->f64, 0, sizeof(double) * filt_len<double>(n, np), c->stream));
+    run = [=]() {
+      if (wantB) blk_mass_cheb<double, double>(st->M64, c->chebB, f.vk, f.w2, f.bwork, c->stream);
+      if (wantA) {
+        if (c->fs) {
+          blk_et<double, double>(st->ET64, f.w2, f.x0, c->stream);
+          blk_ap_cheb_persistent<double, double>(st->Ap64, c->chebAp, f.x0, f.y0, f.apwork, c->bar, c->d_status,
+                                                 st->coop, c->stream);
+        }
+        blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, f.w2, f.y0, f.vkp1, f.vk, f.vkm1, f.yout, ep,
+                                c->stream);
+      }
+    };
+  }
+  if (wantB) {
+    by += dB * b_iter;
+    la += dB;
+  }
+  if (wantA) {
+    by += amv + (c->fs ? et + dAp * ap_iter : 0.0);
+    la += c->fs ? 3 : 1;
+  }
+  for (int i = 0; i < 2; ++i) run();
+  cudaEvent_t e0, e1;
+  NM_CUDA(c, cudaEventCreate(&e0));
+  NM_CUDA(c, cudaEventCreate(&e1));
+  NM_CUDA(c, cudaStreamSynchronize(c->stream));
+  NM_CUDA(c, cudaEventRecord(e0, c->stream));
+  for (int i = 0; i < reps; ++i) run();
+  NM_CUDA(c, cudaEventRecord(e1, c->stream));
+  NM_CUDA(c, cudaEventSynchronize(e1));
+  float t = 0;
+  cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  NM_CUDA(c, cudaGetLastError());
+  if ((rc = check_status(c))) return rc;
+  *ms = t / reps;
+  *bytes = by;
+  *launches_per_op = la;
+  return NM_OK;
+}
+
+int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double** Uout, int* ncout, int* steps_out) {
+  BlockState* st = bs(c);
+  if (!st || !st->ok) return set_err(c, NM_ERR_ARG, "block mode needs the 3-component operator structure");
+  const int n = c->n, np = c->np, S = kBlk;
+  const bool mixed = c->precision == NM_PREC_MIXED;
+  cudaStream_t s = c->stream;
+  int rc;
+  if ((rc = block_buffers(c))) return rc;
+  const size_t L = (size_t)S * n;
   double* p64 = st->f64;
   FiltBufs<double> f64b{};
   if (!mixed) {
@@ -262,6 +366,7 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
                     V.col(0), (int)V.ld));
   // ---- filter graph: zin -> yout (row-major, FP32 or FP64)
   cudaGraphExec_t gexec = nullptr;
+  long long graph_nodes = 0;
   auto run_filter = [&]() {
     if (mixed)
       block_filter<float, float>(c, pol, st->M32, st->A32, st->Ap32, st->E32, st->ET32, f32b);
@@ -270,9 +375,12 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   };
   if (use_graph) {
     cudaGraph_t g;
+    const long long l0 = launches();
     NM_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     run_filter();
     NM_CUDA(c, cudaStreamEndCapture(s, &g));
+    graph_nodes = launches() - l0;
+    add_launches(-graph_nodes);  // captured, not executed
     NM_CUDA(c, cudaGraphInstantiate(&gexec, g, 0));
     cudaGraphDestroy(g);
   }
@@ -347,8 +455,12 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
     // W = F(Z_j)
     if (mixed) blk_gather_cols<float>(Z, j * S, n, f32b.zin, s);
     else blk_gather_cols<double>(Z, j * S, n, f64b.zin, s);
-    if (gexec) NM_CUDA(c, cudaGraphLaunch(gexec, s));
-    else run_filter();
+    if (gexec) {
+      NM_CUDA(c, cudaGraphLaunch(gexec, s));
+      add_launches(graph_nodes);
+    } else {
+      run_filter();
+    }
     c->n_amv += (long long)pol.deg * S;
     c->n_bsolve += (long long)pol.deg * S;
     c->n_spmv += (long long)pol.deg * (c->chebB.deg + (c->fs ? 2 + c->chebAp.deg : 1));

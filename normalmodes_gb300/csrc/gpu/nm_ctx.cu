@@ -346,6 +346,16 @@ int nm_bsolve_block(nm_ctx* c, const double* X, double* Y, int ncols, int ld) {
 
 int nm_time_op(nm_ctx* c, int which, int reps, double* ms_per_op, double* bytes_per_op, int* launches_per_op) {
   if (!c || reps <= 0) return NM_ERR_ARG;
+  if (which >= 4) {
+    double ms = 0, by = 0;
+    int la = 0;
+    int rc = block_time_op(c, which, reps, &ms, &by, &la);
+    if (rc) return rc;
+    if (ms_per_op) *ms_per_op = ms;
+    if (bytes_per_op) *bytes_per_op = by;
+    if (launches_per_op) *launches_per_op = la;
+    return NM_OK;
+  }
   std::vector<double> hx;
   start_vector(hx, c->n, kStartSeed);
   NM_CUDA(c, cudaMemcpy(c->w[0], hx.data(), sizeof(double) * c->n, cudaMemcpyHostToDevice));

@@ -117,6 +117,11 @@ struct nm_ctx {
 
 namespace nmg {
 
+// Kernel launches enqueued by this library (CUDA-graph replays add the
+// captured node count).  Read by nm_solve for nm_result.n_kernels.
+long long launches();
+void add_launches(long long k);
+
 // ---------------------------------------------------------------- status
 int set_err(nm_ctx* c, int code, const std::string& msg);
 #define NM_CUDA(c, call)                                                                 \

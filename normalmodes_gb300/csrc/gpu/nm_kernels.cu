@@ -4,12 +4,18 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <type_traits>
 
 #include "nm_internal.h"
 
 namespace nmg {
+
+static std::atomic<long long> g_launches{0};
+long long launches() { return g_launches.load(); }
+void add_launches(long long k) { g_launches += k; }
+#define NM_COUNT(k) g_launches += (k)
 
 namespace {
 
@@ -430,6 +436,7 @@ void cheb_solve(const Sell<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* 
       k_cheb<VT, XT, false, true><<<nblk(n), kThreads, 0, s>>>(v, b, xi, r, dcur, dnext, x, a, c, it);
     else
       k_cheb<VT, XT, false, false><<<nblk(n), kThreads, 0, s>>>(v, b, xi, r, dcur, dnext, x, a, c, it);
+    NM_COUNT(1);
   }
 }
 template void cheb_solve<double, double>(const Sell<double>&, const ChebSetup&, const double*, double*, double*,
@@ -464,6 +471,7 @@ void cheb_solve_persistent(const Sell<VT>& M, const ChebSetup& ch, const XT* b, 
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   cudaLaunchKernelEx(&cfg, k_cheb_persist<VT, XT>, v, b, x, r, xi, d0, d1, coef, deg, it, bar, status);
+  NM_COUNT(1);
 }
 template void cheb_solve_persistent<double, double>(const Sell<double>&, const ChebSetup&, const double*, double*,
                                                     double*, GridBar*, int*, int, cudaStream_t);
@@ -501,6 +509,7 @@ void amv_fused(const Sell<VT>& A, const Sell<VT>* E, const XT* v, const XT* y, X
     else
       k_amv<VT, XT, false, 1><<<nblk(n), kThreads, 0, s>>>(av, ev, v, y, out, vk, vkm1, yacc, S, CC, PM, MU);
   }
+  NM_COUNT(1);
 }
 template void amv_fused<double, double>(const Sell<double>&, const Sell<double>*, const double*, const double*,
                                         double*, const double*, const double*, double*, const FiltEpi&, cudaStream_t);
@@ -510,31 +519,40 @@ template void amv_fused<float, float>(const Sell<float>&, const Sell<float>*, co
 void dev_fill(double* x, double v, int n, cudaStream_t s) { k_fill<<<nblk(n), kThreads, 0, s>>>(x, v, n); }
 void dev_axpy(double* y, const double* x, double a, int n, cudaStream_t s) {
   k_axpy<<<nblk(n), kThreads, 0, s>>>(y, x, a, n);
+  NM_COUNT(1);
 }
 void dev_axpy_devscal(double* y, const double* x, const double* a, double sign, int n, cudaStream_t s) {
   k_axpy_ds<<<nblk(n), kThreads, 0, s>>>(y, x, a, sign, n);
+  NM_COUNT(1);
 }
 void dev_scale_devscal_inv(double* y, const double* x, const double* a, int n, cudaStream_t s) {
   k_scale_ds_inv<<<nblk(n), kThreads, 0, s>>>(y, x, a, n);
+  NM_COUNT(1);
 }
 void dev_scale(double* y, const double* x, double a, int n, cudaStream_t s) {
   k_scale<<<nblk(n), kThreads, 0, s>>>(y, x, a, n);
+  NM_COUNT(1);
 }
 void dev_mul(double* y, const double* x, const double* d, int n, cudaStream_t s) {
   k_mul<<<nblk(n), kThreads, 0, s>>>(y, x, d, n);
+  NM_COUNT(1);
 }
 void dev_copy(double* y, const double* x, int n, cudaStream_t s) { k_copy<<<nblk(n), kThreads, 0, s>>>(y, x, n); }
 void dev_d2f(float* y, const double* x, int n, cudaStream_t s) { k_d2f<<<nblk(n), kThreads, 0, s>>>(y, x, n); }
 void dev_f2d(double* y, const float* x, int n, cudaStream_t s) { k_f2d<<<nblk(n), kThreads, 0, s>>>(y, x, n); }
 void dev_init_filter(double* vk, double* vkm1, double* y, const double* v, double mu0, int n, cudaStream_t s) {
   k_init_filter<double><<<nblk(n), kThreads, 0, s>>>(vk, vkm1, y, v, mu0, n);
+  NM_COUNT(1);
 }
 void dev_init_filter32(float* vk, float* vkm1, float* y, const float* v, double mu0, int n, cudaStream_t s) {
   k_init_filter<float><<<nblk(n), kThreads, 0, s>>>(vk, vkm1, y, v, (float)mu0, n);
+  NM_COUNT(1);
 }
 void dev_dot(const double* x, const double* y, int n, double* red, double* out, cudaStream_t s) {
   k_dot1<<<kRedBlocks, kThreads, 0, s>>>(x, y, n, red);
+  NM_COUNT(1);
   k_dot2<<<1, kThreads, 0, s>>>(red, kRedBlocks, out);
+  NM_COUNT(1);
 }
 void dev_sqrt_inplace(double* x, cudaStream_t s) { k_sqrt<<<1, 32, 0, s>>>(x); }
 
@@ -544,8 +562,11 @@ void reorth_pass(const Basis& V, const Basis& Z, int ncol, double* z, int n, dou
   if (ncol > kMaxCols) return;
   dim3 g((ncol + kTC - 1) / kTC, kRedParts);
   k_gs_dot<<<g, kThreads, 0, s>>>(V.d_chunks, V.ld, ncol, z, n, red);
+  NM_COUNT(1);
   k_gs_sum<<<nblk(ncol), kThreads, 0, s>>>(red, ncol, h);
+  NM_COUNT(1);
   k_gs_update<<<nblk(n), kThreads, 0, s>>>(Z.d_chunks, Z.ld, ncol, h, z, n);
+  NM_COUNT(1);
 }
 
 }  // namespace nmg

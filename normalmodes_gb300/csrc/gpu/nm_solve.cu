@@ -373,7 +373,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
   const double thr_ext = o.thresh_ext > 0 ? o.thresh_ext : 0.7;
   const bool mixed = c->precision == NM_PREC_MIXED;
   const double t0 = now_s();
-  const long long amv0 = c->n_amv, bs0 = c->n_bsolve, sp0 = c->n_spmv;
+  const long long amv0 = c->n_amv, bs0 = c->n_bsolve, sp0 = c->n_spmv, k0 = launches();
   int rc;
   // ---- bounds of B^-1 A (src/mod_pevsl.f90:84)
   double lmin, lmax;
@@ -434,14 +434,18 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
     dev_scale(Z.col(0), Z.col(0), t, n, c->stream);
     dev_scale(V.col(0), V.col(0), t, n, c->stream);
   }
+  long long graph_nodes = 0;
   double* fin = c->w[2];
   double* fout = c->w[3];
   cudaGraphExec_t gexec = nullptr;
   if (o.use_graph) {
     cudaGraph_t g;
+    const long long l0 = launches();
     NM_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     chebav(c, pol, fin, fout, mixed);
     NM_CUDA(c, cudaStreamEndCapture(c->stream, &g));
+    graph_nodes = launches() - l0;
+    add_launches(-graph_nodes);  // captured, not executed
     NM_CUDA(c, cudaGraphInstantiate(&gexec, g, 0));
     cudaGraphDestroy(g);
     // the capture counted one application; undo so counters reflect launches
@@ -455,6 +459,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
     NM_CUDA(c, cudaMemcpyAsync(fin, Z.col(k), sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
     if (gexec) {
       NM_CUDA(c, cudaGraphLaunch(gexec, c->stream));
+      add_launches(graph_nodes);
       c->n_amv += pol.deg;
       c->n_bsolve += pol.deg;
       c->n_spmv += (long long)pol.deg * (c->chebB.deg + (c->fs ? 2 + c->chebAp.deg : 1));
@@ -516,6 +521,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
     NM_CUDA(c, cudaMemcpyAsync(dS, S.data(), sizeof(double) * (size_t)kdim * nc, cudaMemcpyHostToDevice, c->stream));
     dim3 g(nb(n), (nc + kRitzCols - 1) / kRitzCols);
     k_ritz<<<g, kT, 0, c->stream>>>(V.d_chunks, V.ld, kdim, dS, nc, U, (size_t)n, n);
+    nmg::add_launches(1);
     NM_CUDA(c, cudaStreamSynchronize(c->stream));
     cudaFree(dS);
   }
@@ -539,6 +545,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
       const double th = dot_sync(c, w, u, n);
       if (th < xintv[0] - eps || th > xintv[1] + eps) continue;
       k_resid<<<nb(n), kT, 0, c->stream>>>(w, w2, th, r, n);
+      nmg::add_launches(1);
       const double rn = std::sqrt(dot_sync(c, r, r, n));
       if (!(rn < tol)) continue;
       lam.push_back(th);
@@ -583,6 +590,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
   res->n_amv = c->n_amv - amv0;
   res->n_bsolve = c->n_bsolve - bs0;
   res->n_spmv = c->n_spmv - sp0;
+  res->n_kernels = launches() - k0;
   if (c->verbose) {
     printf(" Relative errors: from the smallest to largest eigens:\n");
     for (int j = 0; j < nev; ++j) printf(" Row %d  relative err. %.6e\n", j + 1, res->err_ref[j]);

@@ -57,7 +57,8 @@ class NmResult(C.Structure):
                 ("lanczos_steps", C.c_int), ("nritz_above_bar", C.c_int),
                 ("t_bounds", C.c_double), ("t_filter_design", C.c_double), ("t_lanczos", C.c_double),
                 ("t_ritz", C.c_double), ("t_total", C.c_double),
-                ("n_amv", C.c_longlong), ("n_bsolve", C.c_longlong), ("n_spmv", C.c_longlong)]
+                ("n_amv", C.c_longlong), ("n_bsolve", C.c_longlong), ("n_spmv", C.c_longlong),
+                ("n_kernels", C.c_longlong)]
 
 
 class NmInfo(C.Structure):
@@ -256,7 +257,7 @@ class Solver:
                                r.pol_bar, r.lanczos_steps, r.nritz_above_bar,
                                {"bounds": r.t_bounds, "filter_design": r.t_filter_design, "lanczos": r.t_lanczos,
                                 "ritz": r.t_ritz, "total": r.t_total},
-                               {"amv": r.n_amv, "bsolve": r.n_bsolve, "spmv": r.n_spmv})
+                               {"amv": r.n_amv, "bsolve": r.n_bsolve, "spmv": r.n_spmv, "kernels": r.n_kernels})
         finally:
             L.nm_result_free(C.byref(r))
 
