@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <type_traits>
 
 #include "nm_block.h"
@@ -189,6 +190,13 @@ __device__ __forceinline__ XT ld(const XT* p) {
 
 // One Chebyshev iteration of the mass solve on a block: rows are 3-DOF
 // groups, t_p = sum_h M_gh x(3h+p, lane).
+// One warp per 3-DOF group row (lane = block column).  The warp loads up to
+// 32 (column, value) entries of its row at once, one per lane, and
+// broadcasts them with shuffles, so the gathers of consecutive entries have
+// no load dependency between them and can be in flight together.  CTAs take
+// consecutive rows; rows are numbered along a space-filling curve, so the
+// rows in flight at any time form a compact piece of the mesh whose
+// neighbour rows stay in L2.
 template <typename VT, typename XT, bool FIRST, bool LAST>
 __global__ void __launch_bounds__(kT)
     k_mass_cheb(int ng, const int* __restrict__ rp, const int* __restrict__ ci, const VT* __restrict__ mv,
@@ -198,30 +206,65 @@ __global__ void __launch_bounds__(kT)
   const int g = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5);
   if (g >= ng) return;
   const XT* src = FIRST ? b : dcur;
+  // own-row state, loaded before the gathers so the loads overlap
+  XT own[3], rold[3], xold[3];
+  const size_t i0 = (size_t)3 * g * kBlk + lane;
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    own[p] = FIRST ? b[i0 + p * kBlk] : dcur[i0 + p * kBlk];
+    rold[p] = FIRST ? own[p] : r[i0 + p * kBlk];
+    xold[p] = FIRST ? (XT)0 : x[i0 + p * kBlk];
+  }
   XT t0 = 0, t1 = 0, t2 = 0;
-  const int e1 = rp[g + 1];
-  for (int e = rp[g]; e < e1; ++e) {
-    const int h = __ldg(ci + e);
-    const XT m = (XT)__ldg(mv + e);
-    const XT* xs = src + (size_t)3 * h * kBlk + lane;
-    t0 = fm<XT>(m, __ldg(xs), t0);
-    t1 = fm<XT>(m, __ldg(xs + kBlk), t1);
-    t2 = fm<XT>(m, __ldg(xs + 2 * kBlk), t2);
+  const int e0 = rp[g], e1 = rp[g + 1];
+  for (int base = e0; base < e1; base += kBlk) {
+    const int cnt = min(kBlk, e1 - base);
+    const int myh = lane < cnt ? __ldg(ci + base + lane) : 0;
+    const XT mym = lane < cnt ? (XT)__ldg(mv + base + lane) : (XT)0;
+    int k = 0;
+    for (; k + 4 <= cnt; k += 4) {
+      const XT* xs[4];
+      XT m[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        xs[u] = src + (size_t)3 * __shfl_sync(0xffffffffu, myh, k + u) * kBlk + lane;
+        m[u] = __shfl_sync(0xffffffffu, mym, k + u);
+      }
+      XT v[4][3];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        v[u][0] = __ldg(xs[u]);
+        v[u][1] = __ldg(xs[u] + kBlk);
+        v[u][2] = __ldg(xs[u] + 2 * kBlk);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        t0 = fm<XT>(m[u], v[u][0], t0);
+        t1 = fm<XT>(m[u], v[u][1], t1);
+        t2 = fm<XT>(m[u], v[u][2], t2);
+      }
+    }
+    for (; k < cnt; ++k) {
+      const XT* xs = src + (size_t)3 * __shfl_sync(0xffffffffu, myh, k) * kBlk + lane;
+      const XT m = __shfl_sync(0xffffffffu, mym, k);
+      t0 = fm<XT>(m, __ldg(xs), t0);
+      t1 = fm<XT>(m, __ldg(xs + kBlk), t1);
+      t2 = fm<XT>(m, __ldg(xs + 2 * kBlk), t2);
+    }
   }
   const XT tt[3] = {t0, t1, t2};
 #pragma unroll
   for (int p = 0; p < 3; ++p) {
-    const size_t idx = ((size_t)3 * g + p) * kBlk + lane;
+    const size_t idx = i0 + p * kBlk;
     XT dc, rr, xn;
     if (FIRST) {
-      const XT bi = b[idx];
-      dc = bi * inv_theta;
-      rr = bi - tt[p] * inv_theta;
+      dc = own[p] * inv_theta;
+      rr = own[p] - tt[p] * inv_theta;
       xn = dc;
     } else {
-      dc = dcur[idx];
-      rr = r[idx] - tt[p];
-      xn = x[idx] + dc;
+      dc = own[p];
+      rr = rold[p] - tt[p];
+      xn = xold[p] + dc;
     }
     const XT dn = fm<XT>(a, dc, c * rr);
     if (LAST) {
@@ -263,12 +306,35 @@ __global__ void __launch_bounds__(kT) k_et(int np, const int* __restrict__ rp, c
   const int k = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5);
   if (k >= np) return;
   XT s = 0;
-  for (int e = rp[k]; e < rp[k + 1]; ++e) {
-    const int h = __ldg(ci + e);
-    const XT* ws = w + (size_t)3 * h * kBlk + lane;
-    s = fm<XT>((XT)__ldg(v3 + 3 * (size_t)e), __ldg(ws), s);
-    s = fm<XT>((XT)__ldg(v3 + 3 * (size_t)e + 1), __ldg(ws + kBlk), s);
-    s = fm<XT>((XT)__ldg(v3 + 3 * (size_t)e + 2), __ldg(ws + 2 * kBlk), s);
+  const int e0 = rp[k], e1 = rp[k + 1];
+  for (int base = e0; base < e1; base += kBlk) {
+    const int cnt = min(kBlk, e1 - base);
+    const int myh = lane < cnt ? __ldg(ci + base + lane) : 0;
+    int q = 0;
+    for (; q + 2 <= cnt; q += 2) {
+      XT w_[2][3];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const XT* ws = w + (size_t)3 * __shfl_sync(0xffffffffu, myh, q + u) * kBlk + lane;
+        w_[u][0] = __ldg(ws);
+        w_[u][1] = __ldg(ws + kBlk);
+        w_[u][2] = __ldg(ws + 2 * kBlk);
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const VT* e3 = v3 + 3 * (size_t)(base + q + u);
+        s = fm<XT>((XT)__ldg(e3), w_[u][0], s);
+        s = fm<XT>((XT)__ldg(e3 + 1), w_[u][1], s);
+        s = fm<XT>((XT)__ldg(e3 + 2), w_[u][2], s);
+      }
+    }
+    for (; q < cnt; ++q) {
+      const XT* ws = w + (size_t)3 * __shfl_sync(0xffffffffu, myh, q) * kBlk + lane;
+      const VT* e3 = v3 + 3 * (size_t)(base + q);
+      s = fm<XT>((XT)__ldg(e3), __ldg(ws), s);
+      s = fm<XT>((XT)__ldg(e3 + 1), __ldg(ws + kBlk), s);
+      s = fm<XT>((XT)__ldg(e3 + 2), __ldg(ws + 2 * kBlk), s);
+    }
   }
   x0[(size_t)k * kBlk + lane] = s;
 }
@@ -307,24 +373,44 @@ __device__ __forceinline__ bool gbar(GridBar* bar, unsigned nblocks, int* status
 
 // Persistent Chebyshev solve on the pressure block: all iterations in one
 // cooperative launch, rows in a grid-stride loop, bounded grid barriers.
+constexpr int kTP = 1024;  // threads of the persistent kernel (one CTA per SM)
+constexpr int kRowsP = kTP / kBlk;
 template <typename VT, typename XT>
-__global__ void __launch_bounds__(kT)
+__global__ void __launch_bounds__(kTP)
     k_ap_cheb(int np, const int* __restrict__ rp, const int* __restrict__ ci, const VT* __restrict__ av,
               const XT* __restrict__ b, XT* xout, XT* r, XT* x, XT* d0, XT* d1, const double* __restrict__ coef,
               int deg, XT inv_theta, GridBar* bar, int* status) {
   const int lane = threadIdx.x & (kBlk - 1);
-  const int rstride = gridDim.x * kRowsPerBlock;
+  const int rstride = gridDim.x * kRowsP;
   for (int k = 0; k < deg; ++k) {
     const XT a = (XT)coef[k], c = (XT)coef[deg + k];
     const XT* dcur = (k & 1) ? d1 : d0;
     XT* dnext = (k & 1) ? d0 : d1;
     const bool first = k == 0, last = k == deg - 1;
-    for (int row = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5); row < np; row += rstride) {
+    for (int row = blockIdx.x * kRowsP + (threadIdx.x >> 5); row < np; row += rstride) {
       const XT* src = first ? b : dcur;
       XT t = 0;
-      for (int e = rp[row]; e < rp[row + 1]; ++e) {
-        const int h = __ldg(ci + e);
-        t = fm<XT>((XT)__ldg(av + e), first ? __ldg(src + (size_t)h * kBlk + lane) : src[(size_t)h * kBlk + lane], t);
+      const int e0 = rp[row], e1 = rp[row + 1];
+      for (int base = e0; base < e1; base += kBlk) {
+        const int cnt = min(kBlk, e1 - base);
+        const int myh = lane < cnt ? __ldg(ci + base + lane) : 0;
+        const XT mya = lane < cnt ? (XT)__ldg(av + base + lane) : (XT)0;
+        int q = 0;
+        for (; q + 4 <= cnt; q += 4) {
+          XT xv[4], m[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const XT* xp = src + (size_t)__shfl_sync(0xffffffffu, myh, q + u) * kBlk + lane;
+            xv[u] = first ? __ldg(xp) : *xp;  // written by other blocks in this launch: coherent load
+            m[u] = __shfl_sync(0xffffffffu, mya, q + u);
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) t = fm<XT>(m[u], xv[u], t);
+        }
+        for (; q < cnt; ++q) {
+          const XT* xp = src + (size_t)__shfl_sync(0xffffffffu, myh, q) * kBlk + lane;
+          t = fm<XT>(__shfl_sync(0xffffffffu, mya, q), first ? __ldg(xp) : *xp, t);
+        }
       }
       const size_t idx = (size_t)row * kBlk + lane;
       XT dc, rr, xn;
@@ -362,20 +448,49 @@ __global__ void __launch_bounds__(kT)
   const int g = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5);
   if (g >= ng) return;
   XT w0 = 0, w1 = 0, w2 = 0;
-  for (int e = arp[g]; e < arp[g + 1]; ++e) {
-    const int h = __ldg(aci + e);
-    const XT* vs = v + (size_t)3 * h * kBlk + lane;
-    const XT x0 = __ldg(vs), x1 = __ldg(vs + kBlk), x2 = __ldg(vs + 2 * kBlk);
-    const VT* a9 = av + 9 * (size_t)e;
-    w0 = fm<XT>((XT)__ldg(a9 + 0), x0, w0);
-    w0 = fm<XT>((XT)__ldg(a9 + 1), x1, w0);
-    w0 = fm<XT>((XT)__ldg(a9 + 2), x2, w0);
-    w1 = fm<XT>((XT)__ldg(a9 + 3), x0, w1);
-    w1 = fm<XT>((XT)__ldg(a9 + 4), x1, w1);
-    w1 = fm<XT>((XT)__ldg(a9 + 5), x2, w1);
-    w2 = fm<XT>((XT)__ldg(a9 + 6), x0, w2);
-    w2 = fm<XT>((XT)__ldg(a9 + 7), x1, w2);
-    w2 = fm<XT>((XT)__ldg(a9 + 8), x2, w2);
+  const int a0 = arp[g], a1 = arp[g + 1];
+  for (int base = a0; base < a1; base += kBlk) {
+    const int cnt = min(kBlk, a1 - base);
+    const int myh = lane < cnt ? __ldg(aci + base + lane) : 0;
+    int k = 0;
+    for (; k + 2 <= cnt; k += 2) {
+      XT xv[2][3];
+      const VT* a9[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const XT* vs = v + (size_t)3 * __shfl_sync(0xffffffffu, myh, k + u) * kBlk + lane;
+        xv[u][0] = __ldg(vs);
+        xv[u][1] = __ldg(vs + kBlk);
+        xv[u][2] = __ldg(vs + 2 * kBlk);
+        a9[u] = av + 9 * (size_t)(base + k + u);
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        w0 = fm<XT>((XT)__ldg(a9[u] + 0), xv[u][0], w0);
+        w0 = fm<XT>((XT)__ldg(a9[u] + 1), xv[u][1], w0);
+        w0 = fm<XT>((XT)__ldg(a9[u] + 2), xv[u][2], w0);
+        w1 = fm<XT>((XT)__ldg(a9[u] + 3), xv[u][0], w1);
+        w1 = fm<XT>((XT)__ldg(a9[u] + 4), xv[u][1], w1);
+        w1 = fm<XT>((XT)__ldg(a9[u] + 5), xv[u][2], w1);
+        w2 = fm<XT>((XT)__ldg(a9[u] + 6), xv[u][0], w2);
+        w2 = fm<XT>((XT)__ldg(a9[u] + 7), xv[u][1], w2);
+        w2 = fm<XT>((XT)__ldg(a9[u] + 8), xv[u][2], w2);
+      }
+    }
+    for (; k < cnt; ++k) {
+      const XT* vs = v + (size_t)3 * __shfl_sync(0xffffffffu, myh, k) * kBlk + lane;
+      const XT x0 = __ldg(vs), x1 = __ldg(vs + kBlk), x2 = __ldg(vs + 2 * kBlk);
+      const VT* a9 = av + 9 * (size_t)(base + k);
+      w0 = fm<XT>((XT)__ldg(a9 + 0), x0, w0);
+      w0 = fm<XT>((XT)__ldg(a9 + 1), x1, w0);
+      w0 = fm<XT>((XT)__ldg(a9 + 2), x2, w0);
+      w1 = fm<XT>((XT)__ldg(a9 + 3), x0, w1);
+      w1 = fm<XT>((XT)__ldg(a9 + 4), x1, w1);
+      w1 = fm<XT>((XT)__ldg(a9 + 5), x2, w1);
+      w2 = fm<XT>((XT)__ldg(a9 + 6), x0, w2);
+      w2 = fm<XT>((XT)__ldg(a9 + 7), x1, w2);
+      w2 = fm<XT>((XT)__ldg(a9 + 8), x2, w2);
+    }
   }
   if (HAS_E) {
     for (int e = erp[g]; e < erp[g + 1]; ++e) {
@@ -511,11 +626,11 @@ void blk_ap_cheb_persistent(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b
   XT* d0 = work + len;
   XT* d1 = work + 2 * len;
   XT* xi = work + 3 * len;
-  blocks = std::max(1, std::min(blocks, nrb(np)));
+  blocks = std::max(1, std::min(blocks, (np + kRowsP - 1) / kRowsP));
   cudaMemsetAsync(bar, 0, sizeof(GridBar), s);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks);
-  cfg.blockDim = dim3(kT);
+  cfg.blockDim = dim3(kTP);
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -529,15 +644,30 @@ void blk_ap_cheb_persistent(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b
   nmg::add_launches(1);
 }
 
+// CTAs of the chunked block kernels: NM_BLK_CTAS_PER_SM (default 8) per SM.
+int blk_grid() {
+  static int g = 0;
+  if (!g) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int per = 8;
+    if (const char* e = std::getenv("NM_BLK_CTAS_PER_SM")) per = std::max(1, std::atoi(e));
+    g = per * sms;
+  }
+  return g;
+}
+
 int blk_coop_blocks() {
   int dev = 0, sms = 0, coop = 0, p64 = 0, p32 = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
   if (!coop) return 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p64, k_ap_cheb<double, double>, kT, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p32, k_ap_cheb<float, float>, kT, 0);
-  return std::min(p64, p32) * sms;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p64, k_ap_cheb<double, double>, kTP, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p32, k_ap_cheb<float, float>, kTP, 0);
+  // one CTA per SM keeps the barrier to one arrival per SM
+  return std::min(1, std::min(p64, p32)) * sms;
 }
 
 template <typename VT, typename XT>

@@ -73,6 +73,7 @@ void blk_init_filter(XT* vk, XT* vkm1, XT* y, const XT* v, double mu0, size_t le
 template <typename XT>
 void blk_from_colmajor(const double* src, size_t ld, int n, XT* blk, cudaStream_t s);  // blk = src(:, 0:S)^T
 int blk_coop_blocks();
+int blk_grid();
 
 // Grouped operators and buffers of the batched path.
 struct BlockState {

@@ -156,8 +156,9 @@ __device__ __forceinline__ bool grid_barrier(GridBar* bar, unsigned nblocks, int
 
 // All `deg` Chebyshev iterations in one launch; rows in a grid-stride loop,
 // a grid barrier between iterations.  Same arithmetic per row as k_cheb.
+constexpr int kThreadsP = 1024;  // persistent kernel: one CTA per SM
 template <typename VT, typename XT>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreadsP)
     k_cheb_persist(SellView<VT> M, const XT* __restrict__ b, XT* xout, XT* r, XT* x, XT* d0, XT* d1,
                    const double* __restrict__ coef,
                    int deg, XT inv_theta, GridBar* bar, int* status) {
@@ -457,12 +458,12 @@ void cheb_solve_persistent(const Sell<VT>& M, const ChebSetup& ch, const XT* b, 
   const XT it = (XT)ch.inv_theta;
   const double* coef = ch.d_coef;
   int deg = ch.deg;
-  blocks = std::min(blocks, nblk(n));
+  blocks = std::min(blocks, nblk(n, kThreadsP));
   if (blocks < 1) blocks = 1;
   cudaMemsetAsync(bar, 0, sizeof(GridBar), s);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks);
-  cfg.blockDim = dim3(kThreads);
+  cfg.blockDim = dim3(kThreadsP);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
@@ -485,9 +486,9 @@ int coop_blocks_for_persistent() {
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
   if (!coop) return 0;
   int p64 = 0, p32 = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p64, k_cheb_persist<double, double>, kThreads, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p32, k_cheb_persist<float, float>, kThreads, 0);
-  per = std::min(p64, p32);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p64, k_cheb_persist<double, double>, kThreadsP, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p32, k_cheb_persist<float, float>, kThreadsP, 0);
+  per = std::min(1, std::min(p64, p32));
   return per * sms;
 }
 

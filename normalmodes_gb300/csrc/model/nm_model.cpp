@@ -490,7 +490,98 @@ void classify_nodes(nmm_model* m, const std::vector<int>& tv) {
   m->np = pacc;
 }
 
-void finish_mesh(nmm_model* m, const std::vector<int>& tv) {
+// Node status from the tetrahedra alone (works for any node numbering):
+// vertices by their incident elements, P2 edge nodes by the statuses of the
+// edge's two vertices (src/mod_geometry.f90:284-312, 672-680).
+void classify_from_tets(nmm_model* m) {
+  const int p = m->pnp;
+  std::vector<char> has_s(m->nnode, 0), has_f(m->nnode, 0), isv(m->nnode, 0);
+  for (int k = 0; k < m->ntet; ++k)
+    for (int v = 0; v < 4; ++v) {
+      const int node = m->tet[(size_t)p * k + m->ref.vord[v]];
+      isv[node] = 1;
+      (m->fluid[k] ? has_f : has_s)[node] = 1;
+    }
+  m->vstat.assign(m->nnode, 0);
+  int maxstat = 0;
+  for (int i = 0; i < m->nnode; ++i)
+    if (isv[i]) {
+      m->vstat[i] = (has_f[i] && !has_s[i]) ? 1 : (has_f[i] && has_s[i]) ? 2 : 0;
+      maxstat = std::max(maxstat, m->vstat[i]);
+    }
+  if (m->porder == 2) {
+    static const int ep[6][2] = {{0, 1}, {0, 2}, {1, 2}, {0, 3}, {1, 3}, {2, 3}};
+    static const int pos_e[6] = {1, 3, 4, 6, 7, 8};
+    for (int k = 0; k < m->ntet; ++k)
+      for (int e = 0; e < 6; ++e) {
+        const int a = m->tet[(size_t)p * k + m->ref.vord[ep[e][0]]];
+        const int b = m->tet[(size_t)p * k + m->ref.vord[ep[e][1]]];
+        const int mn = std::min(m->vstat[a], m->vstat[b]);
+        m->vstat[m->tet[(size_t)p * k + pos_e[e]]] = mn == 0 ? 3 : mn == 1 ? 4 : 5;
+      }
+  }
+  m->fsexist = maxstat == 2;
+  m->purefluid = maxstat == 1;
+  m->rnum.assign(m->nnode, 3);
+  m->pnum.assign(m->nnode, 0);
+  const bool general = m->fsexist || m->purefluid;
+  for (int i = 0; i < m->nnode; ++i) {
+    if (general && (m->vstat[i] == 2 || m->vstat[i] == 5)) m->rnum[i] = 6;
+    if (general && m->vstat[i] != 0 && m->vstat[i] != 3) m->pnum[i] = 1;
+  }
+  m->vstt.assign(m->nnode, 0);
+  m->pstt.assign(m->nnode, -1);
+  int acc = 0, pacc = 0;
+  for (int i = 0; i < m->nnode; ++i) {
+    m->vstt[i] = acc;
+    acc += m->rnum[i];
+    if (m->pnum[i]) m->pstt[i] = pacc++;
+  }
+  m->n = acc;
+  m->np = pacc;
+}
+
+// Renumber nodes along a Morton (Z-order) curve of their doubled grid
+// coordinates, so that consecutive rows of the operators are close in space
+// (the GPU kernels then find a row's neighbours in cache).
+void renumber_morton(nmm_model* m, const std::vector<std::array<int, 3>>& gv) {
+  const int p = m->pnp;
+  std::vector<std::array<int, 3>> g2(m->nnode, {-1, -1, -1});
+  for (int k = 0; k < m->ntet; ++k)
+    for (int v = 0; v < 4; ++v) {
+      const int node = m->tet[(size_t)p * k + m->ref.vord[v]];
+      g2[node] = {2 * gv[node][0], 2 * gv[node][1], 2 * gv[node][2]};
+    }
+  if (m->porder == 2) {
+    static const int ep[6][2] = {{0, 1}, {0, 2}, {1, 2}, {0, 3}, {1, 3}, {2, 3}};
+    static const int pos_e[6] = {1, 3, 4, 6, 7, 8};
+    for (int k = 0; k < m->ntet; ++k)
+      for (int e = 0; e < 6; ++e) {
+        const int a = m->tet[(size_t)p * k + m->ref.vord[ep[e][0]]];
+        const int b = m->tet[(size_t)p * k + m->ref.vord[ep[e][1]]];
+        const int node = m->tet[(size_t)p * k + pos_e[e]];
+        for (int c = 0; c < 3; ++c) g2[node][c] = gv[a][c] + gv[b][c];
+      }
+  }
+  auto spread = [](uint64_t x) {
+    uint64_t r = 0;
+    for (int b = 0; b < 21; ++b) r |= ((x >> b) & 1ull) << (3 * b);
+    return r;
+  };
+  std::vector<std::pair<uint64_t, int>> key(m->nnode);
+  for (int i = 0; i < m->nnode; ++i)
+    key[i] = {spread((uint64_t)g2[i][0]) | (spread((uint64_t)g2[i][1]) << 1) | (spread((uint64_t)g2[i][2]) << 2), i};
+  std::sort(key.begin(), key.end());
+  std::vector<int> newid(m->nnode);
+  for (int r = 0; r < m->nnode; ++r) newid[key[r].second] = r;
+  std::vector<double> xyz(m->xyz.size());
+  for (int i = 0; i < m->nnode; ++i)
+    for (int c = 0; c < 3; ++c) xyz[3 * (size_t)newid[i] + c] = m->xyz[3 * (size_t)i + c];
+  m->xyz.swap(xyz);
+  for (auto& t : m->tet) t = newid[t];
+}
+
+void finish_mesh(nmm_model* m, const std::vector<int>& tv, const std::vector<std::array<int, 3>>* grid = nullptr) {
   if (m->porder == 2) {
     add_p2_nodes(m, tv);
   } else {
@@ -498,7 +589,12 @@ void finish_mesh(nmm_model* m, const std::vector<int>& tv) {
     m->tet = tv;
   }
   mark_boundary_faces(m, tv);
-  classify_nodes(m, tv);
+  if (grid) {
+    std::vector<std::array<int, 3>> gv(m->nnode, {0, 0, 0});
+    for (int i = 0; i < m->nvert; ++i) gv[i] = (*grid)[i];
+    renumber_morton(m, gv);
+  }
+  classify_from_tets(m);
 }
 
 }  // namespace
@@ -679,7 +775,11 @@ int nmm_ball_create(const nmm_ball_opts* o, nmm_model** out) {
   m->xyz = X;
   m->fluid.assign(m->ntet, 0);
   for (int k = 0; k < m->ntet; ++k) m->fluid[k] = (o->fluid_core && layer[k] == 1) ? 1 : 0;
-  finish_mesh(m, tv);
+  std::vector<std::array<int, 3>> grid(m->nvert);
+  for (int i = -mh; i <= mh; ++i)
+    for (int j = -mh; j <= mh; ++j)
+      for (int k = -mh; k <= mh; ++k) grid[vid(i, j, k)] = {i + mh, j + mh, k + mh};
+  finish_mesh(m, tv, &grid);
   // Per-element nodal material.
   ShField fvp, fvs, frho;
   const bool pert = o->lateral_pert != 0.0;
