@@ -118,6 +118,24 @@ int nm_bsolve(nm_ctx* ctx, const double* x, double* y); /* solveBV              
 int nm_amv_dev(nm_ctx* ctx, const double* x, double* y);
 int nm_bmv_dev(nm_ctx* ctx, const double* x, double* y);
 int nm_bsolve_dev(nm_ctx* ctx, const double* x, double* y);
+/* nm_bsolve_dev that allocates nothing.  No counterpart in the reference: it
+ * is an addition of this library for callers that must not allocate device
+ * memory (cudaMalloc/cudaFree can synchronize the device, and a context
+ * sized for the largest models leaves no headroom).  Same arithmetic and
+ * the same result bits as nm_bsolve_dev, enqueued on the context's stream
+ * (no sync); its Chebyshev work vectors live in one scratch array compiled
+ * into the library (4 x NM_NOALLOC_MAX_ROWS doubles = 40 MiB per device),
+ * not in the context.
+ *  - Rejects n > NM_NOALLOC_MAX_ROWS with NM_ERR_ARG (see nm_last_error).
+ *  - The first call on a device looks the scratch address up
+ *    (cudaGetSymbolAddress with the context's device current); make that
+ *    first call before any stream capture.
+ *  - Nothing in the scratch has to start at zero: each call writes every
+ *    row of its work vectors before reading it.
+ *  - All calls on a device share the scratch, across contexts: calls that
+ *    overlap on the GPU race and give undefined results. */
+#define NM_NOALLOC_MAX_ROWS 1310720
+int nm_bsolve_dev_noalloc(nm_ctx* ctx, const double* x, double* y);
 /* Blocks of ncols column vectors with leading dimension ld (host memory). */
 int nm_amv_block(nm_ctx* ctx, const double* X, double* Y, int ncols, int ld);
 int nm_bmv_block(nm_ctx* ctx, const double* X, double* Y, int ncols, int ld);

@@ -30,6 +30,7 @@ EXPORTS = [
     "nm_create", "nm_destroy", "nm_default_opts", "nm_default_solve_opts", "nm_amv", "nm_bmv", "nm_bsolve",
     "nm_amv_dev", "nm_bmv_dev", "nm_bsolve_dev", "nm_amv_block", "nm_bmv_block", "nm_bsolve_block", "nm_solve",
     "nm_result_free", "nm_get_info", "nm_get_stream", "nm_last_error", "nm_sync", "nm_time_op",
+    "nm_bsolve_dev_noalloc",
 ]
 
 
@@ -89,7 +90,8 @@ def lib() -> C.CDLL:
         L.nm_destroy.argtypes = [vp]
         L.nm_default_opts.argtypes = [C.POINTER(NmOpts)]
         L.nm_default_solve_opts.argtypes = [C.POINTER(NmSolveOpts)]
-        for f in ("nm_amv", "nm_bmv", "nm_bsolve", "nm_amv_dev", "nm_bmv_dev", "nm_bsolve_dev"):
+        for f in ("nm_amv", "nm_bmv", "nm_bsolve", "nm_amv_dev", "nm_bmv_dev", "nm_bsolve_dev",
+                  "nm_bsolve_dev_noalloc"):
             getattr(L, f).argtypes = [vp, C.c_void_p, C.c_void_p]
         for f in ("nm_amv_block", "nm_bmv_block", "nm_bsolve_block"):
             getattr(L, f).argtypes = [vp, dp, dp, C.c_int, C.c_int]
