@@ -2,31 +2,37 @@
 """Benchmark of the NormalModes eigensolve on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--precision mixed|fp64] [--block 32|0] [--config 1|0]
+                    [--precision mixed|fp64] [--block 32|0] [--workload NAME]
 
-Workload (configs[1] of the benchmark definition): the seeded 3-layer ball
-(inner core solid, fluid outer core, solid mantle; 36^3 * 6 = 279,936 P2
-tetrahedra, 1,198,455 displacement DOFs + 67,590 pressure DOFs, ~83 nnz per
-row of Ad), all eigenpairs in 0.1-2.0 mHz.  A step is one complete
-polynomial-filtered Lanczos solve of that interval (bounds, filter design,
-filtered Lanczos, Ritz vectors, residual check) with the operators already
-resident in HBM; value = eigenpairs found / time (all ranks).  Every
-operator is larger than L2 (Ad alone is 1.2 GB), so no L2 flush is needed.
+Workload (default "ball36-p2-lateral"): the seeded 3-layer ball (solid inner
+core, fluid outer core, solid mantle; 36^3 * 6 = 279,936 P2 tetrahedra,
+1,198,455 displacement + 67,590 pressure DOFs, ~83 non-zeros per row of Ad)
+with a +-2 % degree-8 lateral perturbation of vp / vs / rho; all eigenpairs
+in 0.1-2.0 mHz.  "ball36-p2" is the same ball without the perturbation,
+"ball12-p1" the small P1 ball (10,368 tetrahedra, 0.2-1.0 mHz) that the CPU
+runs whole.
 
-`e2e` repeats the step through the C-ABI with host buffers: nm_create from
-pinned host CSR arrays (H2D inside the timed region), nm_solve, eigenvalues
-and eigenvectors back to host (D2H), nm_destroy.
+A step is one end-to-end call of the public C-ABI on one spectrum slice:
+nm_create from pinned host CSR arrays (host-to-device copies inside),
+nm_solve (bounds, filter design, filtered Lanczos, Ritz vectors, residual
+check, eigenvectors back to the host), nm_destroy.
+  value : eigenpairs / time of the nm_solve part, timed with CUDA events on
+          the context's stream (operators resident in HBM when it starts);
+  e2e   : eigenpairs / wall time of the whole step.
+Warm-up steps are truncated solves (three block steps, maxit = 96) on a
+context created once, so they run every kernel of the timed step.  Every
+operator and block vector is larger than L2 (Ad alone is 1.2 GB), so no L2
+flush is needed between timed iterations.
 
-`--impl reference` times the CPU path (the FP64 C/OpenMP restatement under
-oracle/, since the Fortran/MPI/pEVSL reference cannot be built here) on a
-bounded sample of the same workload and projects eigenpairs/s; it never
-touches the GPU.
+`--impl reference` times the CPU path of the same workload (the FP64
+C/OpenMP restatement under oracle/ on all host cores, since the
+Fortran/MPI/pEVSL reference cannot be built) on a bounded sample and projects
+eigenpairs/s; it never touches the GPU.
 """
 from __future__ import annotations
 
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -38,15 +44,21 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "eigenpairs/s at resid<=1e-10: mixed+batched vs plain FP64 on GB300; SpMV HBM GB/s"
-CONFIGS = {
-    1: dict(name="configs[1]: layered ball, 279,936 P2 tets, 1.2M DOF, 0.1-2.0 mHz",
-            model=dict(n_cells=36, porder=2), porder=2, interval=(0.1, 2.0)),
-    0: dict(name="configs[0]: layered ball, 10,368 P1 tets, 0.2-1.0 mHz",
-            model=dict(n_cells=12, porder=1), porder=1, interval=(0.2, 1.0)),
+WORKLOADS = {
+    "ball36-p2-lateral": dict(
+        desc="layered ball, 279,936 P2 tets, 1.2M DOF, +-2% degree-8 lateral perturbation, 0.1-2.0 mHz",
+        model=dict(n_cells=36, porder=2, lateral_pert=0.02, lateral_lmax=8), porder=2, interval=(0.1, 2.0)),
+    "ball36-p2": dict(
+        desc="layered ball, 279,936 P2 tets, 1.2M DOF, 0.1-2.0 mHz",
+        model=dict(n_cells=36, porder=2), porder=2, interval=(0.1, 2.0)),
+    "ball12-p1": dict(
+        desc="layered ball, 10,368 P1 tets, 0.2-1.0 mHz",
+        model=dict(n_cells=12, porder=1), porder=1, interval=(0.2, 1.0)),
 }
-# Reference-algorithm step counts of configs[1] measured on GB300 with the
-# single-vector ChebLanNr (used only to scale the CPU samples).
-REF_COUNTS = {1: dict(nev=1232, lanczos_steps=4401, degree=125), 0: None}
+# Step counts of the reference algorithm (single-vector ChebLanNr, FP64) on
+# the 1.2M-DOF ball, measured on GB300; used only to project CPU samples.
+REF_COUNTS = {"ball36-p2-lateral": dict(nev=1232, lanczos_steps=4401, degree=125),
+              "ball36-p2": dict(nev=1232, lanczos_steps=4401, degree=125), "ball12-p1": None}
 
 
 def parse():
@@ -57,8 +69,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--block", type=int, default=32)
-    ap.add_argument("--config", type=int, default=1, choices=[0, 1])
-    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="ball36-p2-lateral", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     return ap.parse_args()
@@ -95,6 +106,16 @@ def allreduce(x: float, ws: int, op: str) -> float:
     t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
     return float(t.item())
+
+
+def aggregate(t_solve: float, t_e2e: float, nev: int, ws: int):
+    """Replicas: every rank solves its own copy of the workload, so the job's
+    time is the slowest rank's and its eigenpairs are the sum over ranks.
+    Returns (value, e2e value, solve seconds, e2e seconds)."""
+    t = allreduce(t_solve, ws, "max")
+    te = allreduce(t_e2e, ws, "max")
+    n_all = allreduce(float(nev), ws, "sum")
+    return n_all / t, n_all / te, t, te
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -161,29 +182,32 @@ def peaks():
 
 
 def traffic_per_launch(key: str):
+    """DRAM bytes (read + write) per launch of `key` from the committed ncu
+    summary (profiles/traffic.json), or None."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(path):
         d = json.load(open(path))
-        v = d.get(key)
-        if v is not None:
-            return float(v)
+        v = d.get(key, {})
+        if isinstance(v, dict) and v.get("bytes_per_launch") is not None:
+            return float(v["bytes_per_launch"])
     return None
 
 
 # ----------------------------------------------------------------------------- CPU sample
-def cpu_sample(cfg_id: int, mats, porder: int, seconds: float, bounds=None):
+def cpu_sample(name: str, mats, porder: int, seconds: float, bounds=None):
     """Time filter degree steps of the FP64 CPU restatement (all host threads)
     and project the reference algorithm's eigenpairs/s for the workload."""
     from oracle import oracle as O
     import numpy as np
+    wl = WORKLOADS[name]
     t0 = time.perf_counter()
     op = O.setup_operator(mats, porder, bounds=bounds)
     t_setup = time.perf_counter() - t0
-    refc = REF_COUNTS.get(cfg_id)
+    refc = REF_COUNTS.get(name)
     if refc is None:
-        # small configuration: the whole reference solve runs on the CPU
+        # small workload: the whole reference solve runs on the CPU
         t1 = time.perf_counter()
-        r = O.apply_pevsl(op, *CONFIGS[cfg_id]["interval"])
+        r = O.apply_pevsl(op, *wl["interval"])
         t_solve = time.perf_counter() - t1
         op.close()
         return {"value": len(r.lam) / t_solve, "unit": "eigenpairs/s", "cores": os.cpu_count(), "kind": "port",
@@ -200,15 +224,12 @@ def cpu_sample(cfg_id: int, mats, porder: int, seconds: float, bounds=None):
         t += time.perf_counter() - t1
         steps += 1
     t_deg = t / steps
-    if refc:
-        t_solve = refc["lanczos_steps"] * refc["degree"] * t_deg
-        value = refc["nev"] / t_solve
-        sample = (f"{steps} filter degree steps (B~^-1 Chebyshev solve of degree {op.b_cheb[2]} + A-op with "
-                  f"Ap Chebyshev of degree {op.ap_cheb[2] if op.ap_cheb else 0}) of the FP64 C/OpenMP restatement "
-                  f"on the full workload, {t_deg:.3f} s each; eigenpairs/s = {refc['nev']} / "
-                  f"({refc['lanczos_steps']} Lanczos steps x degree {refc['degree']} x step time)")
-    else:
-        value, sample = None, f"{steps} filter degree steps, {t_deg:.3f} s each"
+    t_solve = refc["lanczos_steps"] * refc["degree"] * t_deg
+    value = refc["nev"] / t_solve
+    sample = (f"{steps} filter degree steps (B~^-1 Chebyshev solve of degree {op.b_cheb[2]} + A-op with "
+              f"Ap Chebyshev of degree {op.ap_cheb[2] if op.ap_cheb else 0}) of the FP64 C/OpenMP restatement "
+              f"on the full workload, {t_deg:.3f} s each; eigenpairs/s = {refc['nev']} / "
+              f"({refc['lanczos_steps']} Lanczos steps x degree {refc['degree']} x step time)")
     op.close()
     return {"value": value, "unit": "eigenpairs/s", "cores": os.cpu_count(), "kind": "port",
             "sample": sample, "t_degree_step_s": t_deg, "t_setup_s": t_setup}
@@ -218,143 +239,136 @@ def cpu_sample(cfg_id: int, mats, porder: int, seconds: float, bounds=None):
 def main():
     a = parse()
     ws, rank, local = dist_init()
-    cfg = CONFIGS[a.config]
-    lo, hi = cfg["interval"]
+    wl = WORKLOADS[a.workload]
+    lo, hi = wl["interval"]
     from normalmodes_gb300.model import Model
-    mdl = Model.ball(**cfg["model"])
+    mdl = Model.ball(**wl["model"])
     mats = mdl.operators()
     info = mdl.info()
 
     if a.impl == "reference":
         if rank != 0:
             return
-        b = cpu_sample(a.config, mats, cfg["porder"], a.cpu_seconds)
-        for _ in range(a.warmup):
-            pass  # each step is a bounded CPU sample; warm-up is inside cpu_sample
-        vals = [b["value"]]
-        for _ in range(max(0, a.steps - 1)):
-            vals.append(cpu_sample(a.config, mats, cfg["porder"], a.cpu_seconds)["value"])
-        v = statistics.mean(vals) if vals[0] is not None else None
+        vals, b = [], None
+        for _ in range(max(1, a.steps)):
+            b = cpu_sample(a.workload, mats, wl["porder"], a.cpu_seconds)
+            vals.append(b["value"])
+        v = statistics.mean(vals)
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "eigenpairs/s", "n_gpus": a.gpus,
                 "steps": a.steps, "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": cfg["name"], "n_dof": info.n, "n_pressure": info.np},
+                "config": {"workload": wl["desc"], "n_dof": info.n, "n_pressure": info.np},
                 "cpu_baseline": {**b, "value": v},
                 "e2e": {"value": v, "unit": "eigenpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
 
+    import numpy as np
     import torch
-    from normalmodes_gb300 import nmgpu
     from normalmodes_gb300.nmgpu import Solver, NM_PREC_MIXED, NM_PREC_FP64
     prec = NM_PREC_MIXED if a.precision == "mixed" else NM_PREC_FP64
     dev = local
     torch.cuda.set_device(dev)
-    sv = Solver(mats, cfg["porder"], device=dev, precision=prec)
-    sinfo = sv.info()
-    stream = torch.cuda.ExternalStream(sv.stream)
 
-    def solve(s, want_vectors=False):
-        return s.solve(lo, hi, block=a.block, want_vectors=want_vectors)
+    # pinned host copies of the operators: the inputs of every step
+    pinned = {}
+    for k, m in mats.items():
+        pinned[k] = type(m)(torch.from_numpy(m.rowptr).pin_memory().numpy(),
+                            torch.from_numpy(m.col).pin_memory().numpy(),
+                            torch.from_numpy(m.val).pin_memory().numpy(), m.shape)
 
+    # warm-up: truncated solves on one context
+    warm = Solver(pinned, wl["porder"], device=dev, precision=prec)
     for _ in range(a.warmup):
-        solve(sv)
+        warm.solve(lo, hi, block=a.block, maxit=3 * max(a.block, 32), want_vectors=True, unscale=True,
+                   allow_noconv=True)
+    torch.cuda.synchronize()
+
+    nev_tot, kernels, t_solve, h2d, d2h = 0, 0, 0.0, 0, 0
+    res = None
     barrier(ws)
     torch.cuda.synchronize()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    nev_tot, kernels, res = 0, 0, None
     with Clocks(dev) as clk:
-        ev0.record(stream)
+        t0 = time.perf_counter()
         for _ in range(a.steps):
-            res = solve(sv)
+            sv = Solver(pinned, wl["porder"], device=dev, precision=prec)
+            h2d += sv.info().h2d_bytes
+            stream = torch.cuda.ExternalStream(sv.stream)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            res = sv.solve(lo, hi, block=a.block, want_vectors=True, unscale=True)
+            e1.record(stream)
+            e1.synchronize()
+            t_solve += e0.elapsed_time(e1) / 1e3
             nev_tot += len(res.lam)
             kernels += res.counts["kernels"]
-        ev1.record(stream)
+            d2h += 8 * (res.vec.size if res.vec is not None else 0) + 8 * 3 * len(res.lam)
+            sv.close()
         torch.cuda.synchronize()
+        t_e2e = time.perf_counter() - t0
     barrier(ws)
-    t_local = ev0.elapsed_time(ev1) / 1e3
-    t = allreduce(t_local, ws, "max")
-    nev_all = allreduce(float(nev_tot), ws, "sum")
-    value = nev_all / t
     clocks = clk.summary()
+    value, value_e2e, t, te = aggregate(t_solve, t_e2e, nev_tot, ws)
 
-    # roofline of the dominant kernel (block mass Chebyshev step)
+    # roofline of the dominant kernel: the block mass Chebyshev step
+    # (k_mass_cheb, 45 launches per B~^-1 apply), timed live with CUDA events
+    # on the context's stream
     which = 4 if a.block > 1 else 2
-    ms, by, la = sv.time_op(which, 10)
+    ms, by, la = warm.time_op(which, 10)
     per_launch_ms = ms / la
     achieved = (by / la) / (per_launch_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    roof = {"kernel": "k_mass_cheb (block 32, " + ("fp32" if prec == NM_PREC_MIXED else "fp64") + ")"
-            if a.block > 1 else "k_cheb (fp64 SELL)",
-            "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "algorithmic_bytes_per_launch": by / la,
-            "launch_ms": per_launch_ms,
-            "traffic": traffic_per_launch("k_mass_cheb_block32_fp32" if a.block > 1 and prec == NM_PREC_MIXED
-                                          else "k_mass_cheb_block32_fp64" if a.block > 1 else "k_cheb_fp64")}
+    kname = ("k_mass_cheb (block 32, " + ("fp32" if prec == NM_PREC_MIXED else "fp64") + ")" if a.block > 1
+             else "k_cheb (fp64 SELL)")
+    tkey = ("k_mass_cheb_block32_fp32" if prec == NM_PREC_MIXED else "k_mass_cheb_block32_fp64") if a.block > 1 \
+        else "k_cheb_fp64"
+    roof = {"kernel": kname, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+            "algorithmic_bytes_per_launch": by / la, "launch_ms": per_launch_ms,
+            "traffic": traffic_per_launch(tkey)}
     spmv = {}
-    ms_b, by_b, _ = sv.time_op(1, 20)
+    ms_b, by_b, _ = warm.time_op(1, 20)
     spmv["fp64_sell_B_spmv_GBs"] = round(by_b / ms_b / 1e6, 1)
-    ms_f, by_f, la_f = sv.time_op(6 if a.block > 1 else 3, 3)
+    ms_f, by_f, la_f = warm.time_op(6 if a.block > 1 else 3, 3)
     spmv["filter_degree_step_ms"] = round(ms_f, 3)
     spmv["filter_degree_step_GBs"] = round(by_f / ms_f / 1e6, 1)
-
-    # end to end through the C-ABI with host buffers
-    e2e = None
-    if not a.no_e2e:
-        import numpy as np
-        pinned = {}
-        for k, m in mats.items():
-            pinned[k] = type(m)(torch.from_numpy(m.rowptr).pin_memory().numpy(),
-                                torch.from_numpy(m.col).pin_memory().numpy(),
-                                torch.from_numpy(m.val).pin_memory().numpy(), m.shape)
-        barrier(ws)
-        torch.cuda.synchronize()
-        te0 = time.perf_counter()
-        nev_e, h2d, d2h = 0, 0, 0
-        for _ in range(a.steps):
-            s2 = Solver(pinned, cfg["porder"], device=dev, precision=prec)
-            h2d += s2.info().h2d_bytes
-            r2 = s2.solve(lo, hi, block=a.block, want_vectors=True)
-            nev_e += len(r2.lam)
-            d2h += 8 * (r2.vec.size + 3 * len(r2.lam)) if r2.vec is not None else 8 * 3 * len(r2.lam)
-            s2.close()
-        torch.cuda.synchronize()
-        te = allreduce(time.perf_counter() - te0, ws, "max")
-        e2e = {"value": allreduce(float(nev_e), ws, "sum") / te, "unit": "eigenpairs/s",
-               "h2d_bytes_per_step": h2d // a.steps, "d2h_bytes_per_step": d2h // a.steps}
+    winfo = warm.info()
 
     cpu = None
     if rank == 0 and not a.no_cpu:
-        cpu = cpu_sample(a.config, mats, cfg["porder"], a.cpu_seconds,
-                         bounds={"B": tuple(sinfo.b_bounds), "Ap": tuple(sinfo.ap_bounds)} if sinfo.fs else
-                         {"B": tuple(sinfo.b_bounds)})
+        cpu = cpu_sample(a.workload, mats, wl["porder"], a.cpu_seconds,
+                         bounds={"B": tuple(winfo.b_bounds), "Ap": tuple(winfo.ap_bounds)} if winfo.fs else
+                         {"B": tuple(winfo.b_bounds)})
+    warm.close()
     if rank != 0:
-        sv.close()
         return
     line = {
         "metric": METRIC, "value": value, "unit": "eigenpairs/s", "n_gpus": ws, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": t * 1e3 / a.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 filter SpMM / f64 Lanczos, Gram-Schmidt, Rayleigh-Ritz" if prec == NM_PREC_MIXED else "f64",
+        "dtype": "f32 filter SpMM / f64 Lanczos, Rayleigh-Ritz" if prec == NM_PREC_MIXED else "f64",
         "data": "synthetic",
-        "config": {"workload": cfg["name"], "n_dof": info.n, "n_pressure": info.np, "nnz": list(info.nnz),
+        "config": {"workload": wl["desc"], "n_dof": info.n, "n_pressure": info.np, "nnz": list(info.nnz),
                    "interval_mhz": [lo, hi], "precision": a.precision, "block": a.block,
-                   "l2": "operators and vectors exceed L2 (Ad 1.2 GB); no flush",
+                   "l2": "operators and block vectors exceed L2 (Ad 1.2 GB); no flush",
+                   "warmup_steps": "truncated solves (maxit 96)",
                    "eigenpairs_per_step": len(res.lam), "lanczos_vectors": res.lanczos_steps,
-                   "filter_degree": res.pol_deg, "max_err_ref": float(res.err_ref.max()) if len(res.lam) else None,
+                   "filter_degree": res.pol_deg,
+                   "max_err_ref": float(res.err_ref.max()) if len(res.lam) else None,
+                   "median_err_ref": float(np.median(res.err_ref)) if len(res.lam) else None,
                    "max_res2": float(res.res2.max()) if len(res.lam) else None,
                    "parallelism": f"replicas x{ws}"},
         "gpu_launches": kernels,
         "clocks": clocks,
         "roofline": roof,
         "spmv": spmv,
-        "e2e": e2e,
+        "e2e": {"value": value_e2e, "unit": "eigenpairs/s", "h2d_bytes_per_step": h2d // a.steps,
+                "d2h_bytes_per_step": d2h // a.steps},
         "cpu_baseline": cpu,
         "times_s": res.times,
     }
     print(json.dumps(line))
-    sv.close()
 
 
 if __name__ == "__main__":

@@ -95,6 +95,8 @@ typedef struct {
   double t_bounds, t_filter_design, t_lanczos, t_ritz, t_total; /* seconds        */
   long long n_amv, n_bsolve, n_spmv; /* operator applications / SpMV launches       */
   long long n_kernels;   /* kernels of this library launched by the solve            */
+  double t_filter;       /* block path: seconds in the filter applications (CUDA events) */
+  double t_orth;         /* block path: seconds in the block Gram-Schmidt (CUDA events)  */
 } nm_result;
 
 typedef struct nm_ctx nm_ctx;
@@ -144,6 +146,58 @@ int nm_bsolve_block(nm_ctx* ctx, const double* X, double* Y, int ncols, int ld);
 /* The whole solve of pnm_apply_pevsl for [f_lo, f_hi] mHz. */
 int nm_solve(nm_ctx* ctx, double f_lo_mhz, double f_hi_mhz, const nm_solve_opts* opts, nm_result* res);
 void nm_result_free(nm_result* res);
+
+/* Spectrum slicing (the reference runs one interval per job): solves every
+ * slice [f_lo_mhz, f_hi_mhz] on the same context, one after another, with the
+ * same options, into results[i] (nslices results, each freed with
+ * nm_result_free).  Returns NM_OK, the first NM_ERR_NOCONV after finishing
+ * the other slices, or the first other error (results of the slices before
+ * it stay valid). */
+typedef struct {
+  double f_lo_mhz, f_hi_mhz;
+} nm_slice;
+int nm_solve_batched(nm_ctx* ctx, const nm_slice* slices, int nslices, const nm_solve_opts* opts,
+                     nm_result* results);
+
+/* Adjoint sensitivities.  No counterpart in the reference (it has no
+ * gradients); the element model is the mesh, DOF map and nodal material of
+ * the assembly behind the context's operators (nmm_mesh_arrays and
+ * nmm_reference return exactly these arrays).  All host arrays, borrowed for
+ * the call. */
+typedef struct {
+  int ntet, pnp, nnode;
+  int fluid_solid;                  /* 1: fluid-solid (general) model              */
+  const int* tets;                  /* pnp*ntet, reference-element local order     */
+  const double* xyz;                /* 3*nnode                                      */
+  const unsigned char* fluid;       /* ntet                                         */
+  const int* vstt;                  /* nnode: first displacement DOF (solid copy)   */
+  const int* rnum;                  /* nnode: 3, or 6 at fluid-solid nodes          */
+  const int* pstt;                  /* nnode: pressure DOF, -1 if none              */
+  const double *vp, *vs, *rho;      /* pnp*ntet nodal material                      */
+  const double* ref_mass;           /* pnp*pnp, row-major                           */
+  const double* ref_drst;           /* 3*pnp*pnp, d/dr, d/ds, d/dt                  */
+} nm_elem_model;
+
+#define NM_ADJ_PAIR 0      /* one gradient per eigenpair                          */
+#define NM_ADJ_MULTIPLET 1 /* one per group of eigenvalues within tol (relative) */
+
+/* dlam/dm_e = x^T (dA/dm_e - lam dB/dm_e) x for every element e and
+ * m = (density, bulk modulus, shear modulus), where dm_e shifts all nodal
+ * values of m in element e by the same amount and the other two parameters
+ * stay fixed.  For a fluid-solid model x is completed by its pressure
+ * p = -Ap^-1 ET x (the context's Chebyshev approximation of Ap^-1, the same
+ * one its A-operator applies), and the pressure block enters through the
+ * fluid elements' bulk modulus; fluid elements have no shear gradient (0).
+ * The element matrices are recomputed on the GPU, not stored.
+ *   lam : k eigenvalues (ascending), X : n x k unscaled eigenvectors with
+ *         x^T B x = 1 (nm_solve with unscale = 1), column-major, ld ldx.
+ *   grad: (k or ngroups) x ntet x 3 doubles, [.][e][0:rho, 1:kappa, 2:mu].
+ *   group (k ints, may be NULL) receives each pair's group, *ngroups their
+ *   count (a group is a run of consecutive eigenvalues closer than tol,
+ *   relative); NM_ADJ_MULTIPLET sums the pairs of a group (basis-independent for
+ *   a degenerate multiplet). */
+int nm_adjoint(nm_ctx* ctx, const nm_elem_model* em, int k, const double* lam, const double* X, int ldx, int mode,
+               double tol, double* grad, int* group, int* ngroups);
 
 /* Introspection. */
 typedef struct {

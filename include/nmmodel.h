@@ -105,6 +105,11 @@ int nmm_mesh_arrays(const nmm_model* m, const double** xyz, const int** tets,
                     const int** rnum, const int** pstt, const double** vp,
                     const double** vs, const double** rho);
 
+/* Replace the per-element nodal material (pnp*ntet values each, copied) and
+ * mark the model for re-assembly.  The solid / fluid classification of every
+ * element must stay as it is (NMM_ERR_ARG otherwise). */
+int nmm_set_material(nmm_model* m, const double* vp, const double* vs, const double* rho);
+
 /* Element matrices of tet k exactly as the assembly scatters them:
  * solid: TM, MM are (3 pnp)^2 row-major; fluid: FT, FM are (3 pnp + pnp)^2.
  * *dim receives the matrix dimension. */

@@ -160,6 +160,92 @@ int upload_g(nm_ctx* c, const GCsrHost& h, GCsr<T>& d) {
 template int upload_g<double>(nm_ctx*, const GCsrHost&, GCsr<double>&);
 template int upload_g<float>(nm_ctx*, const GCsrHost&, GCsr<float>&);
 
+bool tile_csr(const GCsrHost& g, int R, TCsrHost& t) {
+  if (g.bs != 1 || R <= 0) return false;
+  t = TCsrHost();
+  t.nrows = g.nrows;
+  t.R = R;
+  t.ntiles = (g.nrows + R - 1) / R;
+  t.rp = g.rp;
+  t.v = g.v;
+  t.li.resize(g.ci.size());
+  std::vector<std::vector<int>> U(t.ntiles);
+  bool ok = true;
+#pragma omp parallel for schedule(dynamic, 64) reduction(&& : ok)
+  for (int k = 0; k < t.ntiles; ++k) {
+    const int r0 = k * R, r1 = std::min(r0 + R, g.nrows);
+    std::vector<int>& u = U[k];
+    u.assign(g.ci.begin() + g.rp[r0], g.ci.begin() + g.rp[r1]);
+    std::sort(u.begin(), u.end());
+    u.erase(std::unique(u.begin(), u.end()), u.end());
+    if (u.size() > 65535) {
+      ok = false;
+      continue;
+    }
+    for (int e = g.rp[r0]; e < g.rp[r1]; ++e)
+      t.li[e] = (uint16_t)(std::lower_bound(u.begin(), u.end(), g.ci[e]) - u.begin());
+  }
+  if (!ok) return false;
+  t.tptr.assign(t.ntiles + 1, 0);
+  for (int k = 0; k < t.ntiles; ++k) {
+    t.tptr[k + 1] = t.tptr[k] + (int)U[k].size();
+    t.maxU = std::max(t.maxU, (int)U[k].size());
+  }
+  t.ulist.resize(t.tptr[t.ntiles]);
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < t.ntiles; ++k) std::copy(U[k].begin(), U[k].end(), t.ulist.begin() + t.tptr[k]);
+  return true;
+}
+
+int tile_rows_for(const GCsrHost& g, int R0, size_t row_bytes, size_t smem_max, TCsrHost& t) {
+  for (int R = R0; R >= 4; R /= 2) {
+    if (!tile_csr(g, R, t)) continue;
+    if ((size_t)t.maxU * row_bytes <= smem_max) return R;
+  }
+  t = TCsrHost();
+  return 0;
+}
+
+template <typename T>
+int upload_t(nm_ctx* c, const TCsrHost& h, TCsr<T>& d) {
+  free_t(d);
+  d.nrows = h.nrows;
+  d.R = h.R;
+  d.ntiles = h.ntiles;
+  d.maxU = h.maxU;
+  d.nnz = (long long)h.li.size();
+  d.nu = (long long)h.ulist.size();
+  NM_CUDA(c, cudaMalloc(&d.tptr, sizeof(int) * (h.ntiles + 1)));
+  NM_CUDA(c, cudaMalloc(&d.ulist, sizeof(int) * std::max<long long>(d.nu, 1)));
+  NM_CUDA(c, cudaMalloc(&d.rp, sizeof(int) * (h.nrows + 1)));
+  NM_CUDA(c, cudaMalloc(&d.li, sizeof(uint16_t) * std::max<long long>(d.nnz, 1)));
+  NM_CUDA(c, cudaMalloc(&d.v, sizeof(T) * std::max<long long>(d.nnz, 1)));
+  NM_CUDA(c, cudaMemcpy(d.tptr, h.tptr.data(), sizeof(int) * (h.ntiles + 1), cudaMemcpyHostToDevice));
+  if (d.nu) NM_CUDA(c, cudaMemcpy(d.ulist, h.ulist.data(), sizeof(int) * d.nu, cudaMemcpyHostToDevice));
+  NM_CUDA(c, cudaMemcpy(d.rp, h.rp.data(), sizeof(int) * (h.nrows + 1), cudaMemcpyHostToDevice));
+  if (d.nnz) {
+    NM_CUDA(c, cudaMemcpy(d.li, h.li.data(), sizeof(uint16_t) * d.nnz, cudaMemcpyHostToDevice));
+    std::vector<T> tmp(h.v.begin(), h.v.end());
+    NM_CUDA(c, cudaMemcpy(d.v, tmp.data(), sizeof(T) * d.nnz, cudaMemcpyHostToDevice));
+  }
+  c->dev_bytes += d.bytes();
+  return NM_OK;
+}
+template int upload_t<float>(nm_ctx*, const TCsrHost&, TCsr<float>&);
+template int upload_t<double>(nm_ctx*, const TCsrHost&, TCsr<double>&);
+
+template <typename T>
+void free_t(TCsr<T>& t) {
+  cudaFree(t.tptr);
+  cudaFree(t.ulist);
+  cudaFree(t.rp);
+  cudaFree(t.li);
+  cudaFree(t.v);
+  t = TCsr<T>();
+}
+template void free_t<float>(TCsr<float>&);
+template void free_t<double>(TCsr<double>&);
+
 template <typename T>
 void free_g(GCsr<T>& g) {
   cudaFree(g.rp);
@@ -188,34 +274,49 @@ __device__ __forceinline__ XT ld(const XT* p) {
   return __ldg(p);
 }
 
-// One Chebyshev iteration of the mass solve on a block: rows are 3-DOF
-// groups, t_p = sum_h M_gh x(3h+p, lane).
-// One warp per 3-DOF group row (lane = block column).  The warp loads up to
-// 32 (column, value) entries of its row at once, one per lane, and
-// broadcasts them with shuffles, so the gathers of consecutive entries have
-// no load dependency between them and can be in flight together.  CTAs take
-// consecutive rows; rows are numbered along a space-filling curve, so the
-// rows in flight at any time form a compact piece of the mesh whose
-// neighbour rows stay in L2.
-template <typename VT, typename XT, bool FIRST, bool LAST>
-__global__ void __launch_bounds__(kT)
+// One Chebyshev iteration of the mass solve on a block, three-term form.
+// With x_0 = 0 and x_1 = b / theta, the semi-iteration
+//   x_{j+1} = x_j + a_{j-1} (x_j - x_{j-1}) + c_{j-1} (b - M x_j)
+// is the same polynomial in M as the residual / direction form
+// (x += d, r -= M d, d = a d + c r) with the same a, c, but it streams four
+// blocks per step (gather x_j, own x_{j-1}, own b, write x_{j+1}) instead of
+// six.  MODE 0: j = 1 (x_j = b / theta, x_{j-1} = 0); MODE 1: j = 2
+// (x_{j-1} = b / theta); MODE 2: general.  xprev and xout may alias: each
+// row is read and then written by the thread that owns it, and no thread
+// gathers from that buffer in the same step.
+// Rows are 3-DOF groups, t_p = sum_h M_gh x(3h+p, lane); one warp per group
+// row (lane = block column).  The warp loads up to 32 (column, value)
+// entries of its row at once, one per lane, and broadcasts them with
+// shuffles, so the gathers of consecutive entries have no load dependency
+// between them and can be in flight together.  CTAs take consecutive rows;
+// rows are numbered along a space-filling curve, so the rows in flight at
+// any time form a compact piece of the mesh whose neighbour rows stay in L2.
+// LATE: the own-row state is read after the gathers instead of before, and
+// registers are capped for full occupancy (more rows in flight per SM
+// instead of more loads in flight per row).
+template <typename VT, typename XT, int NC, int MODE, bool LATE = false>
+__global__ void __launch_bounds__(kT, LATE ? 8 : 1)
     k_mass_cheb(int ng, const int* __restrict__ rp, const int* __restrict__ ci, const VT* __restrict__ mv,
-                const XT* __restrict__ b, XT* __restrict__ x, XT* __restrict__ r, const XT* __restrict__ dcur,
-                XT* __restrict__ dnext, XT* __restrict__ xout, XT a, XT c, XT inv_theta) {
+                const XT* __restrict__ b, const XT* __restrict__ xcur, const XT* xprev, XT* xout, XT a, XT c,
+                XT inv_theta) {
   const int lane = threadIdx.x & (kBlk - 1);
-  const int g = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5);
+  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (g >= ng) return;
-  const XT* src = FIRST ? b : dcur;
-  // own-row state, loaded before the gathers so the loads overlap
-  XT own[3], rold[3], xold[3];
-  const size_t i0 = (size_t)3 * g * kBlk + lane;
+  const XT* src = MODE == 0 ? b : xcur;
+  XT bo[NC], xc[NC], xp[NC];
+  const size_t i0 = (size_t)NC * g * kBlk + lane;
+  auto load_own = [&]() {
 #pragma unroll
-  for (int p = 0; p < 3; ++p) {
-    own[p] = FIRST ? b[i0 + p * kBlk] : dcur[i0 + p * kBlk];
-    rold[p] = FIRST ? own[p] : r[i0 + p * kBlk];
-    xold[p] = FIRST ? (XT)0 : x[i0 + p * kBlk];
-  }
-  XT t0 = 0, t1 = 0, t2 = 0;
+    for (int p = 0; p < NC; ++p) {
+      bo[p] = b[i0 + p * kBlk];
+      xc[p] = MODE == 0 ? bo[p] * inv_theta : xcur[i0 + p * kBlk];
+      xp[p] = MODE == 0 ? (XT)0 : MODE == 1 ? bo[p] * inv_theta : xprev[i0 + p * kBlk];
+    }
+  };
+  if (!LATE) load_own();  // issued before the gathers so the loads overlap
+  XT t[NC];
+#pragma unroll
+  for (int p = 0; p < NC; ++p) t[p] = 0;
   const int e0 = rp[g], e1 = rp[g + 1];
   for (int base = e0; base < e1; base += kBlk) {
     const int cnt = min(kBlk, e1 - base);
@@ -227,52 +328,242 @@ __global__ void __launch_bounds__(kT)
       XT m[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        xs[u] = src + (size_t)3 * __shfl_sync(0xffffffffu, myh, k + u) * kBlk + lane;
+        xs[u] = src + (size_t)NC * __shfl_sync(0xffffffffu, myh, k + u) * kBlk + lane;
         m[u] = __shfl_sync(0xffffffffu, mym, k + u);
       }
-      XT v[4][3];
+      XT v[4][NC];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        v[u][0] = __ldg(xs[u]);
-        v[u][1] = __ldg(xs[u] + kBlk);
-        v[u][2] = __ldg(xs[u] + 2 * kBlk);
-      }
+      for (int u = 0; u < 4; ++u)
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        t0 = fm<XT>(m[u], v[u][0], t0);
-        t1 = fm<XT>(m[u], v[u][1], t1);
-        t2 = fm<XT>(m[u], v[u][2], t2);
-      }
+        for (int p = 0; p < NC; ++p) v[u][p] = __ldg(xs[u] + p * kBlk);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int p = 0; p < NC; ++p) t[p] = fm<XT>(m[u], v[u][p], t[p]);
     }
     for (; k < cnt; ++k) {
-      const XT* xs = src + (size_t)3 * __shfl_sync(0xffffffffu, myh, k) * kBlk + lane;
+      const XT* xs = src + (size_t)NC * __shfl_sync(0xffffffffu, myh, k) * kBlk + lane;
       const XT m = __shfl_sync(0xffffffffu, mym, k);
-      t0 = fm<XT>(m, __ldg(xs), t0);
-      t1 = fm<XT>(m, __ldg(xs + kBlk), t1);
-      t2 = fm<XT>(m, __ldg(xs + 2 * kBlk), t2);
+#pragma unroll
+      for (int p = 0; p < NC; ++p) t[p] = fm<XT>(m, __ldg(xs + p * kBlk), t[p]);
     }
   }
-  const XT tt[3] = {t0, t1, t2};
+  if (LATE) load_own();
 #pragma unroll
-  for (int p = 0; p < 3; ++p) {
-    const size_t idx = i0 + p * kBlk;
-    XT dc, rr, xn;
-    if (FIRST) {
-      dc = own[p] * inv_theta;
-      rr = own[p] - tt[p] * inv_theta;
-      xn = dc;
-    } else {
-      dc = own[p];
-      rr = rold[p] - tt[p];
-      xn = xold[p] + dc;
+  for (int p = 0; p < NC; ++p) {
+    const XT tt = MODE == 0 ? t[p] * inv_theta : t[p];
+    // x_{j+1} = x_j + a (x_j - x_{j-1}) + c (b - M x_j)
+    xout[i0 + p * kBlk] = fm<XT>(c, bo[p] - tt, fm<XT>(a, xc[p] - xp[p], xc[p]));
+  }
+}
+
+// Vector-load variant of the gather Chebyshev step (same recurrence, MODE
+// convention and results up to rounding).  A warp still owns one row, but
+// each neighbour row of the block (NC * 32 values) is read with 16-byte
+// loads by LPN = 32 / V lanes (V values per load), so one warp instruction
+// fetches SLOTS = V neighbour rows at once: lane (q, i) accumulates columns
+// V*i .. V*i+V-1 over the neighbours k with k % SLOTS == q, and the SLOTS
+// partial sums are combined with shuffles at the end.  Four times fewer load
+// instructions than the scalar-lane kernel for FP32.
+template <typename XT>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using T = float4;
+  static constexpr int V = 4;
+};
+template <>
+struct Vec16<double> {
+  using T = double2;
+  static constexpr int V = 2;
+};
+template <typename VT4, typename XT>
+__device__ __forceinline__ void vfma(XT m, const VT4& x, XT* acc);
+template <>
+__device__ __forceinline__ void vfma<float4, float>(float m, const float4& x, float* acc) {
+  acc[0] = fmaf(m, x.x, acc[0]);
+  acc[1] = fmaf(m, x.y, acc[1]);
+  acc[2] = fmaf(m, x.z, acc[2]);
+  acc[3] = fmaf(m, x.w, acc[3]);
+}
+template <>
+__device__ __forceinline__ void vfma<double2, double>(double m, const double2& x, double* acc) {
+  acc[0] = fma(m, x.x, acc[0]);
+  acc[1] = fma(m, x.y, acc[1]);
+}
+template <typename VT4>
+__device__ __forceinline__ VT4 ldv(const VT4* p) {
+  return __ldg(p);
+}
+
+template <typename VT, typename XT, int NC, int MODE>
+__global__ void __launch_bounds__(kT)
+    k_gcheb(int ng, const int* __restrict__ rp, const int* __restrict__ ci, const VT* __restrict__ mv,
+            const XT* __restrict__ b, const XT* __restrict__ xcur, const XT* xprev, XT* xout, XT a, XT c,
+            XT inv_theta) {
+  using V4 = typename Vec16<XT>::T;
+  constexpr int V = Vec16<XT>::V;
+  constexpr int LPN = kBlk / V;      // lanes per neighbour row (per component)
+  constexpr int SLOTS = 32 / LPN;    // neighbour rows per warp instruction
+  constexpr int RW = NC * kBlk;      // values per block row
+  const int lane = threadIdx.x & 31;
+  const int q = lane / LPN, i = lane % LPN;
+  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (g >= ng) return;
+  const XT* src = MODE == 0 ? b : xcur;
+  XT acc[NC][V];
+#pragma unroll
+  for (int p = 0; p < NC; ++p)
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[p][v] = 0;
+  const int e0 = rp[g], e1 = rp[g + 1];
+  for (int base = e0; base < e1; base += 32) {
+    const int cnt = min(32, e1 - base);
+    const int myh = lane < cnt ? __ldg(ci + base + lane) : g;
+    const XT mym = lane < cnt ? (XT)__ldg(mv + base + lane) : (XT)0;
+    for (int k = 0; k < cnt; k += 2 * SLOTS) {
+      // two rounds of SLOTS neighbours in flight; entries past cnt carry m = 0
+      const int k0 = k + q, k1 = k + SLOTS + q;
+      const int h0 = __shfl_sync(0xffffffffu, myh, k0 & 31), h1 = __shfl_sync(0xffffffffu, myh, k1 & 31);
+      const XT m0 = __shfl_sync(0xffffffffu, mym, k0 & 31), m1 = __shfl_sync(0xffffffffu, mym, k1 & 31);
+      const XT w0 = k0 < cnt ? m0 : (XT)0, w1 = k1 < cnt ? m1 : (XT)0;
+      const V4* p0 = reinterpret_cast<const V4*>(src + (size_t)(k0 < cnt ? h0 : g) * RW) + i;
+      const V4* p1 = reinterpret_cast<const V4*>(src + (size_t)(k1 < cnt ? h1 : g) * RW) + i;
+      V4 x0[NC], x1[NC];
+#pragma unroll
+      for (int p = 0; p < NC; ++p) {
+        x0[p] = ldv(p0 + p * LPN);
+        x1[p] = ldv(p1 + p * LPN);
+      }
+#pragma unroll
+      for (int p = 0; p < NC; ++p) {
+        vfma<V4, XT>(w0, x0[p], acc[p]);
+        vfma<V4, XT>(w1, x1[p], acc[p]);
+      }
     }
-    const XT dn = fm<XT>(a, dc, c * rr);
-    if (LAST) {
-      xout[idx] = xn + dn;
-    } else {
-      r[idx] = rr;
-      x[idx] = xn;
-      dnext[idx] = dn;
+  }
+  // combine the SLOTS partial sums (butterfly: every lane gets the total)
+#pragma unroll
+  for (int o = LPN; o < 32; o <<= 1)
+#pragma unroll
+    for (int p = 0; p < NC; ++p)
+#pragma unroll
+      for (int v = 0; v < V; ++v) acc[p][v] += __shfl_xor_sync(0xffffffffu, acc[p][v], o);
+  // epilogue: lane (q, i) writes components q, q + SLOTS, ..., columns V*i ..
+#pragma unroll
+  for (int pq = 0; pq < NC; pq += SLOTS) {
+    const int cq = pq + q;
+    if (cq >= NC) break;
+    XT t[V];
+#pragma unroll
+    for (int p = 0; p < NC; ++p)
+      if (p == cq) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) t[v] = acc[p][v];
+      }
+    const size_t o = (size_t)g * RW + (size_t)cq * kBlk + (size_t)i * V;
+    const V4 bo = *reinterpret_cast<const V4*>(b + o);
+    const XT* bs = reinterpret_cast<const XT*>(&bo);
+    V4 xc4, xp4;
+    if (MODE != 0) xc4 = *reinterpret_cast<const V4*>(xcur + o);
+    if (MODE == 2) xp4 = *reinterpret_cast<const V4*>(xprev + o);
+    const XT* xcs = reinterpret_cast<const XT*>(&xc4);
+    const XT* xps = reinterpret_cast<const XT*>(&xp4);
+    V4 out;
+    XT* os = reinterpret_cast<XT*>(&out);
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const XT xc = MODE == 0 ? bs[v] * inv_theta : xcs[v];
+      const XT xp = MODE == 0 ? (XT)0 : MODE == 1 ? bs[v] * inv_theta : xps[v];
+      const XT tt = MODE == 0 ? t[v] * inv_theta : t[v];
+      os[v] = fm<XT>(c, bs[v] - tt, fm<XT>(a, xc - xp, xc));
+    }
+    *reinterpret_cast<V4*>(xout + o) = out;
+  }
+}
+
+// Staged (tiled) three-term Chebyshev step on a block with NC components
+// per row; same recurrence and MODE convention as k_mass_cheb.  One CTA per
+// tile of R rows: it first copies the tile's distinct neighbour rows of the
+// gathered block (NC * 32 values each) into shared memory with cp.async
+// (16-byte pieces, all in flight at once), then each warp computes its rows
+// from shared memory (one row per warp, lane = block column; the row's
+// (local column, value) entries are broadcast with shuffles).
+constexpr int kTT = 256;  // threads of the staged kernel
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+template <typename VT, typename XT, int NC, int MODE>
+__global__ void __launch_bounds__(kTT)
+    k_tcheb(int nrows, int R, const int* __restrict__ tptr, const int* __restrict__ ulist,
+            const int* __restrict__ rp, const uint16_t* __restrict__ li, const VT* __restrict__ mv,
+            const XT* __restrict__ b, const XT* __restrict__ xcur, const XT* xprev, XT* xout, XT a, XT c,
+            XT inv_theta) {
+  extern __shared__ __align__(16) unsigned char tc_smem[];
+  XT* sx = reinterpret_cast<XT*>(tc_smem);
+  constexpr int RW = NC * kBlk;                 // values per staged row
+  constexpr int V = 16 / (int)sizeof(XT);       // values per 16-byte piece
+  constexpr int PIECES = RW / V;                // pieces per staged row
+  const int tile = blockIdx.x;
+  const int u0 = tptr[tile], nu = tptr[tile + 1] - u0;
+  const XT* src = MODE == 0 ? b : xcur;
+  for (int i = threadIdx.x; i < nu * PIECES; i += kTT) {
+    const int u = i / PIECES, q = i - u * PIECES;
+    const int h = __ldg(ulist + u0 + u);
+    cp_async16(sx + (size_t)u * RW + q * V, src + (size_t)h * RW + q * V);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int r0 = tile * R, r1 = min(r0 + R, nrows);
+  for (int row = r0 + warp; row < r1; row += kTT / 32) {
+    const size_t i0 = (size_t)row * RW + lane;
+    XT bo[NC], xc[NC], xp[NC], t[NC];
+#pragma unroll
+    for (int p = 0; p < NC; ++p) {
+      bo[p] = b[i0 + p * kBlk];
+      xc[p] = MODE == 0 ? bo[p] * inv_theta : xcur[i0 + p * kBlk];
+      xp[p] = MODE == 0 ? (XT)0 : MODE == 1 ? bo[p] * inv_theta : xprev[i0 + p * kBlk];
+      t[p] = 0;
+    }
+    const int e0 = rp[row], e1 = rp[row + 1];
+    for (int base = e0; base < e1; base += 32) {
+      const int cnt = min(32, e1 - base);
+      const int myl = lane < cnt ? (int)__ldg(li + base + lane) : 0;
+      const XT mym = lane < cnt ? (XT)__ldg(mv + base + lane) : (XT)0;
+      int k = 0;
+      for (; k + 4 <= cnt; k += 4) {
+        XT m[4], v[4][NC];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const XT* sp = sx + __shfl_sync(0xffffffffu, myl, k + u) * RW + lane;
+          m[u] = __shfl_sync(0xffffffffu, mym, k + u);
+#pragma unroll
+          for (int p = 0; p < NC; ++p) v[u][p] = sp[p * kBlk];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int p = 0; p < NC; ++p) t[p] = fm<XT>(m[u], v[u][p], t[p]);
+      }
+      for (; k < cnt; ++k) {
+        const XT* sp = sx + __shfl_sync(0xffffffffu, myl, k) * RW + lane;
+        const XT m = __shfl_sync(0xffffffffu, mym, k);
+#pragma unroll
+        for (int p = 0; p < NC; ++p) t[p] = fm<XT>(m, sp[p * kBlk], t[p]);
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < NC; ++p) {
+      const XT tt = MODE == 0 ? t[p] * inv_theta : t[p];
+      xout[i0 + p * kBlk] = fm<XT>(c, bo[p] - tt, fm<XT>(a, xc[p] - xp[p], xc[p]));
     }
   }
 }
@@ -579,30 +870,138 @@ __global__ void k_init_filter_blk(XT* vk, XT* vkm1, XT* y, const XT* v, XT mu0, 
 
 }  // namespace
 
-template <typename VT, typename XT>
-void blk_mass_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s) {
+// Threads per CTA of the gather Chebyshev kernel (one row per warp).
+int gather_threads() {
+  static int t = 0;
+  if (!t) {
+    t = kT;
+    if (const char* e = std::getenv("NM_GATHER_THREADS")) t = std::min(kT, std::max(32, std::atoi(e) / 32 * 32));
+  }
+  return t;
+}
+
+// Gather kernel per component count: the 16-byte vector-load kernel
+// (k_gcheb) measured faster for one-component rows (Ap, 128-byte rows), the
+// one-value-per-lane kernel (k_mass_cheb) for the three-component mass rows.
+// NM_GATHER_VEC=0/1 forces one of them for measurements.
+bool gather_vec(int nc) {
+  static int v = -2;
+  if (v == -2) {
+    v = -1;
+    if (const char* e = std::getenv("NM_GATHER_VEC")) v = std::atoi(e) != 0;
+  }
+  return v < 0 ? nc == 1 : v != 0;
+}
+
+// Register-capped late-load variant of k_mass_cheb (NM_MASS_LATE=1).
+bool gather_late() {
+  static int v = -1;
+  if (v < 0) {
+    v = 0;
+    if (const char* e = std::getenv("NM_MASS_LATE")) v = std::atoi(e) != 0;
+  }
+  return v != 0;
+}
+
+template <typename VT, typename XT, int NC>
+void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s) {
   const int ng = M.nrows;
-  const size_t len = (size_t)3 * ng * kBlk;
-  XT* r = work;
-  XT* d0 = work + len;
-  XT* d1 = work + 2 * len;
-  XT* xi = work + 3 * len;
+  if (ng == 0 || ch.deg == 0) return;
+  const size_t len = (size_t)NC * ng * kBlk;
+  XT* buf[2] = {work, work + len};  // x_j lives in buf[j & 1]
   const XT it = (XT)ch.inv_theta;
-  for (int k = 0; k < ch.deg; ++k) {
-    const XT a = (XT)ch.a[k], c = (XT)ch.c[k];
-    const bool first = k == 0, last = k == ch.deg - 1;
-    XT* dcur = (k & 1) ? d1 : d0;
-    XT* dnext = (k & 1) ? d0 : d1;
-#define NM_MC(F, L) \
-  k_mass_cheb<VT, XT, F, L><<<nrb(ng), kT, 0, s>>>(ng, M.rp, M.ci, M.v, b, xi, r, dcur, dnext, x, a, c, it)
-    if (first && last) NM_MC(true, true);
-    else if (first) NM_MC(true, false);
-    else if (last) NM_MC(false, true);
-    else NM_MC(false, false);
+  const int thr = gather_threads(), rows = thr / 32;
+  const int grid = (ng + rows - 1) / rows;
+  for (int j = 1; j <= ch.deg; ++j) {
+    const XT a = (XT)ch.a[j - 1], c = (XT)ch.c[j - 1];
+    XT* out = j == ch.deg ? x : buf[(j + 1) & 1];
+    const XT* cur = buf[j & 1];
+    const XT* prev = buf[(j + 1) & 1];
+#define NM_MC(K, MODE) K<VT, XT, NC, MODE><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it)
+    if (gather_vec(NC)) {
+      if (j == 1) NM_MC(k_gcheb, 0);
+      else if (j == 2) NM_MC(k_gcheb, 1);
+      else NM_MC(k_gcheb, 2);
+    } else if (gather_late()) {
+#define NM_ML(MODE) \
+  k_mass_cheb<VT, XT, NC, MODE, true><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it)
+      if (j == 1) NM_ML(0);
+      else if (j == 2) NM_ML(1);
+      else NM_ML(2);
+#undef NM_ML
+    } else {
+      if (j == 1) NM_MC(k_mass_cheb, 0);
+      else if (j == 2) NM_MC(k_mass_cheb, 1);
+      else NM_MC(k_mass_cheb, 2);
+    }
 #undef NM_MC
     nmg::add_launches(1);
   }
 }
+
+template <typename VT, typename XT>
+void blk_mass_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s) {
+  gather_cheb<VT, XT, 3>(M, ch, b, x, work, s);
+}
+
+template <typename VT, typename XT>
+void blk_ap_cheb(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s) {
+  gather_cheb<VT, XT, 1>(Ap, ch, b, x, work, s);
+}
+
+void blk_prefer_l1() {
+  for (const void* f : {(const void*)k_mass_cheb<float, float, 3, 0>, (const void*)k_mass_cheb<float, float, 3, 1>,
+                        (const void*)k_mass_cheb<float, float, 3, 2>, (const void*)k_mass_cheb<float, float, 1, 0>,
+                        (const void*)k_mass_cheb<float, float, 1, 1>, (const void*)k_mass_cheb<float, float, 1, 2>,
+                        (const void*)k_mass_cheb<double, double, 3, 0>, (const void*)k_mass_cheb<double, double, 3, 1>,
+                        (const void*)k_mass_cheb<double, double, 3, 2>, (const void*)k_mass_cheb<double, double, 1, 0>,
+                        (const void*)k_mass_cheb<double, double, 1, 1>, (const void*)k_mass_cheb<double, double, 1, 2>})
+    cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  cudaGetLastError();
+}
+
+template <typename VT, typename XT, int NC>
+size_t blk_tcheb_smem(const TCsr<VT>& T) {
+  const size_t bytes = (size_t)T.maxU * NC * kBlk * sizeof(XT);
+  if (bytes > 227 * 1024) return 0;
+  // opt in to the shared memory of the largest tile for every MODE instance
+  // (on the current device; called once per context, before any capture)
+  const int lim = (int)std::max<size_t>(bytes, 1);
+  if (cudaFuncSetAttribute(k_tcheb<VT, XT, NC, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
+      cudaFuncSetAttribute(k_tcheb<VT, XT, NC, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
+      cudaFuncSetAttribute(k_tcheb<VT, XT, NC, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess)
+    return 0;
+  return bytes;
+}
+
+template <typename VT, typename XT, int NC>
+void blk_tcheb(const TCsr<VT>& T, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s) {
+  if (T.nrows == 0 || ch.deg == 0) return;
+  const size_t len = (size_t)NC * T.nrows * kBlk;
+  XT* buf[2] = {work, work + len};  // x_j lives in buf[j & 1]
+  const XT it = (XT)ch.inv_theta;
+  const size_t smem = (size_t)T.maxU * NC * kBlk * sizeof(XT);
+  for (int j = 1; j <= ch.deg; ++j) {
+    const XT a = (XT)ch.a[j - 1], c = (XT)ch.c[j - 1];
+    XT* out = j == ch.deg ? x : buf[(j + 1) & 1];
+    const XT* cur = buf[j & 1];
+    const XT* prev = buf[(j + 1) & 1];
+#define NM_TC(MODE)                                                                                             \
+  k_tcheb<VT, XT, NC, MODE><<<T.ntiles, kTT, smem, s>>>(T.nrows, T.R, T.tptr, T.ulist, T.rp, T.li, T.v, b, cur, \
+                                                         prev, out, a, c, it)
+    if (j == 1) NM_TC(0);
+    else if (j == 2) NM_TC(1);
+    else NM_TC(2);
+#undef NM_TC
+    nmg::add_launches(1);
+  }
+}
+template void blk_tcheb<float, float, 3>(const TCsr<float>&, const ChebSetup&, const float*, float*, float*,
+                                         cudaStream_t);
+template void blk_tcheb<float, float, 1>(const TCsr<float>&, const ChebSetup&, const float*, float*, float*,
+                                         cudaStream_t);
+template size_t blk_tcheb_smem<float, float, 3>(const TCsr<float>&);
+template size_t blk_tcheb_smem<float, float, 1>(const TCsr<float>&);
 
 template <typename VT>
 void blk_mass_spmv(const GCsr<VT>& M, const double* x, double* y, cudaStream_t s) {
@@ -697,6 +1096,34 @@ void blk_gather_cols(const Basis& Z, int j0, int n, XT* blk, cudaStream_t s) {
   k_gather_cols<XT><<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(Z.d_chunks, Z.ld, j0, n, blk);
   nmg::add_launches(1);
 }
+namespace {
+__global__ void k_d2f(const double* __restrict__ src, size_t lds, float* __restrict__ dst, size_t ldd, int n,
+                      int cols) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * cols) return;
+  const int c = (int)(t / n), i = (int)(t % n);
+  dst[(size_t)c * ldd + i] = (float)src[(size_t)c * lds + i];
+}
+__global__ void k_sub_f32(double* __restrict__ W, size_t ldw, const float* __restrict__ T, size_t ldt, int n,
+                          int cols) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * cols) return;
+  const int c = (int)(t / n), i = (int)(t % n);
+  W[(size_t)c * ldw + i] -= (double)T[(size_t)c * ldt + i];
+}
+}  // namespace
+
+void blk_d2f(const double* src, size_t lds, float* dst, size_t ldd, int n, int cols, cudaStream_t s) {
+  const long long tot = (long long)n * cols;
+  k_d2f<<<(int)((tot + 255) / 256), 256, 0, s>>>(src, lds, dst, ldd, n, cols);
+  nmg::add_launches(1);
+}
+void blk_sub_f32(double* W, size_t ldw, const float* T, size_t ldt, int n, int cols, cudaStream_t s) {
+  const long long tot = (long long)n * cols;
+  k_sub_f32<<<(int)((tot + 255) / 256), 256, 0, s>>>(W, ldw, T, ldt, n, cols);
+  nmg::add_launches(1);
+}
+
 template <typename XT>
 void blk_to_colmajor(const XT* blk, int n, double* out, size_t ld, cudaStream_t s) {
   k_to_colmajor<XT><<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(blk, n, out, ld);
@@ -718,6 +1145,7 @@ void blk_init_filter(XT* vk, XT* vkm1, XT* y, const XT* v, double mu0, size_t le
 
 #define NM_INST(VT, XT)                                                                                              \
   template void blk_mass_cheb<VT, XT>(const GCsr<VT>&, const ChebSetup&, const XT*, XT*, XT*, cudaStream_t);        \
+  template void blk_ap_cheb<VT, XT>(const GCsr<VT>&, const ChebSetup&, const XT*, XT*, XT*, cudaStream_t);          \
   template void blk_et<VT, XT>(const GCsr<VT>&, const XT*, XT*, cudaStream_t);                                     \
   template void blk_ap_cheb_persistent<VT, XT>(const GCsr<VT>&, const ChebSetup&, const XT*, XT*, XT*, GridBar*,   \
                                                int*, int, cudaStream_t);                                           \

@@ -37,6 +37,42 @@ struct GCsrHost {
   std::vector<double> v;
 };
 
+// Row-tiled scalar CSR for the shared-memory staged block SpMM.  Rows are
+// cut into tiles of R consecutive rows; ulist[tptr[t] .. tptr[t+1]) holds the
+// distinct columns that tile t touches (ascending) and li[e] the position of
+// entry e's column in that list, so one CTA stages the tile's neighbour rows
+// of the block once in shared memory and every entry then reads shared
+// memory instead of gathering from L2.
+template <typename T>
+struct TCsr {
+  int nrows = 0, R = 0, ntiles = 0, maxU = 0;
+  long long nnz = 0, nu = 0;
+  int* tptr = nullptr;
+  int* ulist = nullptr;
+  int* rp = nullptr;
+  uint16_t* li = nullptr;
+  T* v = nullptr;
+  size_t bytes() const {
+    return (size_t)(ntiles + 1) * 4 + (size_t)nu * 4 + (size_t)(nrows + 1) * 4 + (size_t)nnz * (2 + sizeof(T));
+  }
+};
+struct TCsrHost {
+  int nrows = 0, R = 0, ntiles = 0, maxU = 0;
+  std::vector<int> tptr, ulist, rp;
+  std::vector<uint16_t> li;
+  std::vector<double> v;
+};
+// Tiles of R rows of a scalar grouped CSR (bs == 1); false if a tile would
+// touch more than 65535 distinct columns.
+bool tile_csr(const GCsrHost& g, int R, TCsrHost& t);
+template <typename T>
+int upload_t(nm_ctx* c, const TCsrHost& h, TCsr<T>& d);
+template <typename T>
+void free_t(TCsr<T>& t);
+// Largest R (halving from R0) whose staged tile fits `smem_max` bytes with
+// `row_bytes` per staged row.
+int tile_rows_for(const GCsrHost& g, int R0, size_t row_bytes, size_t smem_max, TCsrHost& t);
+
 // Host extraction from scaled DOF-level CSR; false if the structure is absent.
 bool group_mass(const nm_csr* B, const std::vector<double>& D, GCsrHost& M);
 bool group_bsr3(const nm_csr* A, const std::vector<double>& dl, const std::vector<double>& dr, GCsrHost& G);
@@ -54,6 +90,10 @@ void free_g(GCsr<T>& g);
 template <typename VT, typename XT>
 void blk_mass_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s);
 template <typename VT, typename XT>
+void blk_ap_cheb(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s);
+// Prefer L1 over shared memory for the gather kernels (once per context).
+void blk_prefer_l1();
+template <typename VT, typename XT>
 void blk_et(const GCsr<VT>& ET, const XT* w, XT* x0, cudaStream_t s);
 template <typename VT, typename XT>
 void blk_ap_cheb_persistent(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b, XT* x, XT* work, GridBar* bar,
@@ -61,6 +101,14 @@ void blk_ap_cheb_persistent(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b
 template <typename VT, typename XT>
 void blk_amv(const GCsr<VT>& A, const GCsr<VT>* E, const XT* v, const XT* y, XT* out, const XT* vk, const XT* vkm1,
              XT* yacc, const FiltEpi& ep, cudaStream_t s);
+// Chebyshev solve (three-term form, deg launches) of the block with NC
+// components per row on a tiled matrix: NC = 3 for the mass M (x) I_3,
+// NC = 1 for the pressure matrix Ap.  work holds 2 blocks.
+template <typename VT, typename XT, int NC>
+void blk_tcheb(const TCsr<VT>& T, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s);
+// Shared-memory bytes one CTA of blk_tcheb needs (0 if the tiles do not fit).
+template <typename VT, typename XT, int NC>
+size_t blk_tcheb_smem(const TCsr<VT>& T);
 template <typename VT>
 void blk_mass_spmv(const GCsr<VT>& M, const double* x, double* y, cudaStream_t s);
 // Conversions between basis columns (FP64, column-major chunks) and row-major blocks.
@@ -75,13 +123,31 @@ void blk_from_colmajor(const double* src, size_t ld, int n, XT* blk, cudaStream_
 int blk_coop_blocks();
 int blk_grid();
 
+// FP32 copy of a Lanczos basis (chunks of Basis::kChunk columns, ld = n
+// rounded up to 32), the operand of the mixed path's Gram-Schmidt GEMMs.
+struct Basis32 {
+  int n = 0;
+  size_t ld = 0;
+  std::vector<float*> chunks;
+  float* col(int j) const { return chunks[j / Basis::kChunk] + (size_t)(j % Basis::kChunk) * ld; }
+};
+// Column-major conversions of S-column blocks: dst = (float)src; W -= T.
+void blk_d2f(const double* src, size_t lds, float* dst, size_t ldd, int n, int cols, cudaStream_t s);
+void blk_sub_f32(double* W, size_t ldw, const float* T, size_t ldt, int n, int cols, cudaStream_t s);
+
 // Grouped operators and buffers of the batched path.
 struct BlockState {
   bool ok = false;
   GCsr<double> M64, A64, E64, ET64, Ap64;
   GCsr<float> M32, A32, E32, ET32, Ap32;
+  TCsr<float> TM32, TAp32;  // tiled copies for the staged FP32 Chebyshev solves
+  bool tiled = false;
   float* f32 = nullptr;
   double* f64 = nullptr;
+  Basis32 V32, Z32;  // FP32 copies of the basis (mixed path)
+  // Chebyshev set-ups of the FP32 filter's inner solves (degrees matched to
+  // FP32 accuracy; mixed path only, set by block_buffers)
+  ChebSetup chB32, chAp32;
   size_t f32_len = 0, f64_len = 0;
   cublasHandle_t cublas = nullptr;
   cusolverDnHandle_t cusolver = nullptr;
@@ -93,7 +159,8 @@ int block_build(nm_ctx* c, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, c
 void block_free(nm_ctx* c);
 // Block filtered Lanczos; on success U (n x nc, column-major, device, owned
 // by the caller) holds the Ritz vectors with p(theta) >= bar.
-int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double** U, int* nc, int* steps);
+int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double** U, int* nc, int* steps,
+                  double* t_filter, double* t_orth);
 // FP64 Rayleigh-Ritz on the columns of U (n x nc): U <- U Q with
 // (U^T A U) Q = (U^T B U) Q Theta.  Resolves the mixing of close Ritz pairs
 // left by an FP32 filter.

@@ -13,8 +13,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <type_traits>
 #include <vector>
 
 #include "nm_block.h"
@@ -75,6 +77,26 @@ int block_build(nm_ctx* c, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, c
         ((rc = upload_g(c, hE, st->E32)) || (rc = upload_g(c, hET, st->ET32)) || (rc = upload_g(c, hAp, st->Ap32))))
       return rc;
   }
+  if (c->precision == NM_PREC_MIXED) {
+    // staged FP32 Chebyshev solves: tiles of consecutive rows whose distinct
+    // neighbour rows fit in shared memory (R halves until they fit)
+    const size_t smem_max = 110 * 1024;
+    int rM = 32, rAp = 32;
+    if (const char* e = std::getenv("NM_TILE_ROWS_M")) rM = std::max(4, std::atoi(e));
+    if (const char* e = std::getenv("NM_TILE_ROWS_AP")) rAp = std::max(4, std::atoi(e));
+    TCsrHost tM, tAp;
+    bool tiled = tile_rows_for(hM, rM, 3 * kBlk * sizeof(float), smem_max, tM) > 0;
+    if (tiled && c->fs) tiled = tile_rows_for(hAp, rAp, kBlk * sizeof(float), smem_max, tAp) > 0;
+    if (tiled) {
+      if ((rc = upload_t(c, tM, st->TM32))) return rc;
+      if (c->fs && (rc = upload_t(c, tAp, st->TAp32))) return rc;
+      tiled = blk_tcheb_smem<float, float, 3>(st->TM32) > 0 &&
+              (!c->fs || blk_tcheb_smem<float, float, 1>(st->TAp32) > 0);
+      cudaGetLastError();
+    }
+    st->tiled = tiled && std::getenv("NM_NO_TILES") == nullptr;
+  }
+  blk_prefer_l1();
   st->coop = blk_coop_blocks();
   st->ok = true;
   return NM_OK;
@@ -85,6 +107,10 @@ void block_free(nm_ctx* c) {
   if (!st) return;
   for (auto* g : {&st->M64, &st->A64, &st->E64, &st->ET64, &st->Ap64}) free_g(*g);
   for (auto* g : {&st->M32, &st->A32, &st->E32, &st->ET32, &st->Ap32}) free_g(*g);
+  free_t(st->TM32);
+  free_t(st->TAp32);
+  for (float* q : st->V32.chunks) cudaFree(q);
+  for (float* q : st->Z32.chunks) cudaFree(q);
   cudaFree(st->f32);
   cudaFree(st->f64);
   if (st->cublas) cublasDestroy(st->cublas);
@@ -131,6 +157,69 @@ FiltBufs<XT> filt_carve(XT* base, size_t n, size_t np) {
   return f;
 }
 
+// Kernel choice of the block Chebyshev solves.  0: gather kernel (one row
+// per warp, neighbour rows from L1/L2); 1: staged kernel (tile's neighbour
+// rows copied to shared memory, FP32 only); 2: persistent single-launch
+// kernel (Ap only).  Overridable for measurements with NM_MASS_KERNEL and
+// NM_AP_KERNEL.
+int kernel_choice(const char* env, int dflt) {
+  if (const char* e = std::getenv(env)) return std::atoi(e);
+  return dflt;
+}
+
+// The FP32 filter's inner Chebyshev solves use the degrees of chB32 / chAp32
+// (FP32 accuracy); FP64 solves the reference's degrees.
+template <typename XT>
+const ChebSetup& mass_cheb(nm_ctx* c) {
+  BlockState* st = bs(c);
+  return std::is_same<XT, float>::value && st->chB32.deg > 0 ? st->chB32 : c->chebB;
+}
+template <typename XT>
+const ChebSetup& ap_cheb(nm_ctx* c) {
+  BlockState* st = bs(c);
+  return std::is_same<XT, float>::value && st->chAp32.deg > 0 ? st->chAp32 : c->chebAp;
+}
+
+template <typename VT, typename XT>
+void blk_mass_solve(nm_ctx* c, const GCsr<VT>& M, const XT* b, XT* x, XT* work) {
+  BlockState* st = bs(c);
+  static const int kind = kernel_choice("NM_MASS_KERNEL", 0);
+  if constexpr (std::is_same<XT, float>::value && std::is_same<VT, float>::value) {
+    if (st->tiled && kind == 1) {
+      blk_tcheb<float, float, 3>(st->TM32, mass_cheb<XT>(c), b, x, work, c->stream);
+      return;
+    }
+  }
+  blk_mass_cheb<VT, XT>(M, mass_cheb<XT>(c), b, x, work, c->stream);
+}
+template <typename VT, typename XT>
+void blk_ap_solve(nm_ctx* c, const GCsr<VT>& Ap, const XT* b, XT* x, XT* work) {
+  BlockState* st = bs(c);
+  static const int kind = kernel_choice("NM_AP_KERNEL", 0);
+  if constexpr (std::is_same<XT, float>::value && std::is_same<VT, float>::value) {
+    if (st->tiled && kind == 1) {
+      blk_tcheb<float, float, 1>(st->TAp32, ap_cheb<XT>(c), b, x, work, c->stream);
+      return;
+    }
+  }
+  if (kind == 2 && st->coop > 0)  // the persistent kernel reads the reference set-up's device coefficients
+    blk_ap_cheb_persistent<VT, XT>(Ap, c->chebAp, b, x, work, c->bar, c->d_status, st->coop, c->stream);
+  else
+    blk_ap_cheb<VT, XT>(Ap, ap_cheb<XT>(c), b, x, work, c->stream);
+}
+
+// Degree at which the Chebyshev semi-iteration on [lmin, lmax] reaches the
+// relative error eps: 2 sigma^d <= eps, sigma = (sqrt(k) - 1) / (sqrt(k) + 1),
+// k = lmax / lmin (Golub & Varga); never above the reference's degree.
+int cheb_degree_for(const ChebSetup& ref, double eps) {
+  if (!(ref.lmin > 0.0) || !(ref.lmax > ref.lmin)) return ref.deg;
+  const double k = ref.lmax / ref.lmin, sk = std::sqrt(k);
+  const double sigma = (sk - 1.0) / (sk + 1.0);
+  if (!(sigma > 0.0)) return std::min(ref.deg, 1);
+  const int d = (int)std::ceil(std::log(eps / 2.0) / std::log(sigma));
+  return std::max(1, std::min(ref.deg, d));
+}
+
 template <typename VT, typename XT>
 void block_filter(nm_ctx* c, const Pol& pol, const GCsr<VT>& M, const GCsr<VT>& A, const GCsr<VT>& Ap,
                   const GCsr<VT>& E, const GCsr<VT>& ET, FiltBufs<XT> f) {
@@ -140,10 +229,10 @@ void block_filter(nm_ctx* c, const Pol& pol, const GCsr<VT>& M, const GCsr<VT>& 
   blk_init_filter<XT>(f.vk, f.vkm1, f.yout, f.zin, pol.mu[0], L, s);
   XT *vk = f.vk, *vkm1 = f.vkm1, *vkp1 = f.vkp1;
   for (int k = 1; k <= pol.deg; ++k) {
-    blk_mass_cheb<VT, XT>(M, c->chebB, vk, f.w2, f.bwork, s);
+    blk_mass_solve<VT, XT>(c, M, vk, f.w2, f.bwork);
     if (c->fs) {
       blk_et<VT, XT>(ET, f.w2, f.x0, s);
-      blk_ap_cheb_persistent<VT, XT>(Ap, c->chebAp, f.x0, f.y0, f.apwork, c->bar, c->d_status, st->coop, s);
+      blk_ap_solve<VT, XT>(c, Ap, f.x0, f.y0, f.apwork);
     }
     FiltEpi ep;
     ep.mode = 1;
@@ -169,6 +258,23 @@ int block_buffers(nm_ctx* c) {
   if (!st->cublas) {
     CB(c, cublasCreate(&st->cublas));
     CS(c, cusolverDnCreate(&st->cusolver));
+  }
+  if (mixed && st->chB32.deg == 0 && std::getenv("NM_FILTER_FULL_DEG") == nullptr) {
+    // FP32 filter: inner Chebyshev solves to FP32 accuracy (2^-24)
+    const double eps32 = 5.9604644775390625e-08;
+    st->chB32 = c->chebB;
+    st->chB32.d_coef = nullptr;
+    st->chB32.deg = cheb_degree_for(c->chebB, eps32);
+    cheb_coefs(st->chB32);
+    if (c->fs) {
+      st->chAp32 = c->chebAp;
+      st->chAp32.d_coef = nullptr;
+      st->chAp32.deg = cheb_degree_for(c->chebAp, eps32);
+      cheb_coefs(st->chAp32);
+    }
+    if (c->verbose)
+      printf(" FP32 filter: B Chebyshev degree %d (reference %d), Ap %d (reference %d)\n", st->chB32.deg,
+             c->chebB.deg, st->chAp32.deg, c->chebAp.deg);
   }
   CB(c, cublasSetStream(st->cublas, c->stream));
   CS(c, cusolverDnSetStream(st->cusolver, c->stream));
@@ -211,10 +317,18 @@ int block_time_op(nm_ctx* c, int which, int reps, double* ms, double* bytes, int
   const long long nnzE = c->fs ? (mixed ? st->E32.nnz : st->E64.nnz) : 0;
   const long long nnzET = c->fs ? (mixed ? st->ET32.nnz : st->ET64.nnz) : 0;
   const long long nnzAp = c->fs ? (mixed ? st->Ap32.nnz : st->Ap64.nnz) : 0;
-  const int dB = c->chebB.deg, dAp = c->chebAp.deg;
-  // per Chebyshev step on the mass: matrix + row pointers + 6 vector streams
-  const double b_iter = (double)nnzM * (vs + 4) + (double)(n / 3 + 1) * 4 + 6.0 * L * xs;
-  const double ap_iter = c->fs ? (double)nnzAp * (vs + 4) + (double)(np + 1) * 4 + 6.0 * P * xs : 0.0;
+  const int dB = mixed ? mass_cheb<float>(c).deg : c->chebB.deg;
+  const int dAp = mixed ? ap_cheb<float>(c).deg : c->chebAp.deg;
+  // Chebyshev solve in the three-term form: every step reads the matrix and
+  // row pointers once; block streams per step: step 1 gathers b and writes
+  // (2), step 2 gathers x_j, reads b and writes (3), later steps also read
+  // x_{j-1} (4)
+  auto cheb_streams = [](int deg) { return deg <= 0 ? 0.0 : deg == 1 ? 2.0 : 5.0 + 4.0 * (deg - 2); };
+  const double b_mat = (double)nnzM * (vs + 4) + (double)(n / 3 + 1) * 4;
+  // Ap Chebyshev solve: three-term multi-launch form, or the persistent
+  // residual / direction form (6 streams per step)
+  const bool tiled = !(kernel_choice("NM_AP_KERNEL", 0) == 2 && st->coop > 0);
+  const double ap_mat = c->fs ? (double)nnzAp * (vs + 4) + (double)(np + 1) * 4 : 0.0;
   const double et = c->fs ? (double)nnzET * (3 * vs + 4) + (double)(np + 1) * 4 + L * xs + P * xs : 0.0;
   const double amv = (double)nnzA * (9 * vs + 4) + (double)(n / 3 + 1) * 4 + (double)nnzE * (3 * vs + 4) +
                      L * xs /* v */ + (c->fs ? P * xs : 0.0) + 4.0 * L * xs /* vk, vkm1, out, yacc */;
@@ -232,12 +346,11 @@ int block_time_op(nm_ctx* c, int which, int reps, double* ms, double* bytes, int
     FiltBufs<float> f = filt_carve<float>(st->f32, n, np);
     NM_CUDA(c, cudaMemsetAsync(st->f32, 0, sizeof(float) * st->f32_len, c->stream));
     run = [=]() {
-      if (wantB) blk_mass_cheb<float, float>(st->M32, c->chebB, f.vk, f.w2, f.bwork, c->stream);
+      if (wantB) blk_mass_solve<float, float>(c, st->M32, f.vk, f.w2, f.bwork);
       if (wantA) {
         if (c->fs) {
           blk_et<float, float>(st->ET32, f.w2, f.x0, c->stream);
-          blk_ap_cheb_persistent<float, float>(st->Ap32, c->chebAp, f.x0, f.y0, f.apwork, c->bar, c->d_status,
-                                               st->coop, c->stream);
+          blk_ap_solve<float, float>(c, st->Ap32, f.x0, f.y0, f.apwork);
         }
         blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, f.vkp1, f.vk, f.vkm1, f.yout, ep,
                               c->stream);
@@ -260,12 +373,13 @@ int block_time_op(nm_ctx* c, int which, int reps, double* ms, double* bytes, int
     };
   }
   if (wantB) {
-    by += dB * b_iter;
+    by += dB * b_mat + cheb_streams(dB) * L * xs;
     la += dB;
   }
   if (wantA) {
-    by += amv + (c->fs ? et + dAp * ap_iter : 0.0);
-    la += c->fs ? 3 : 1;
+    const double ap = c->fs ? dAp * ap_mat + (tiled ? cheb_streams(dAp) : 6.0 * dAp) * P * xs : 0.0;
+    by += amv + (c->fs ? et + ap : 0.0);
+    la += c->fs ? (tiled ? 2 + dAp : 3) : 1;
   }
   for (int i = 0; i < 2; ++i) run();
   cudaEvent_t e0, e1;
@@ -288,7 +402,29 @@ int block_time_op(nm_ctx* c, int which, int reps, double* ms, double* bytes, int
   return NM_OK;
 }
 
-int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double** Uout, int* ncout, int* steps_out) {
+namespace {
+// Grow an FP32 basis copy to at least ncols columns.
+int ensure32(nm_ctx* c, Basis32& b, int n, int ncols) {
+  if (b.n == 0) {
+    b.n = n;
+    b.ld = ((size_t)n + 31) / 32 * 32;
+  }
+  const int need = (ncols + Basis::kChunk - 1) / Basis::kChunk;
+  while ((int)b.chunks.size() < need) {
+    float* p = nullptr;
+    if (cudaMalloc(&p, b.ld * Basis::kChunk * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      return NM_ERR_OOM;
+    }
+    b.chunks.push_back(p);
+    c->dev_bytes += b.ld * Basis::kChunk * sizeof(float);
+  }
+  return NM_OK;
+}
+}  // namespace
+
+int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double** Uout, int* ncout, int* steps_out,
+                  double* t_filter, double* t_orth) {
   BlockState* st = bs(c);
   if (!st || !st->ok) return set_err(c, NM_ERR_ARG, "block mode needs the 3-component operator structure");
   const int n = c->n, np = c->np, S = kBlk;
@@ -331,6 +467,38 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   }
   const double one = 1.0, mone = -1.0, zero = 0.0;
   cublasHandle_t hb = st->cublas;
+  // Mixed path: the block Gram-Schmidt against the basis runs as FP32 GEMMs
+  // on FP32 copies of V and Z (the filter output carries FP32 rounding
+  // already, and FP32 projections keep the basis orthogonal to ~1e-7, far
+  // below what the Lanczos recurrence needs to stay free of ghost copies);
+  // W itself, the three-term recurrence, the Cholesky and the basis stay
+  // FP64.  The FP64 GEMMs are the fallback when the FP32 copy cannot grow.
+  bool orth32 = mixed && std::getenv("NM_ORTH64") == nullptr;
+  float *W32 = nullptr, *T32 = nullptr, *dH32 = nullptr;
+  if (orth32) {
+    if (cudaMalloc(&W32, sizeof(float) * L) != cudaSuccess || cudaMalloc(&T32, sizeof(float) * L) != cudaSuccess ||
+        cudaMalloc(&dH32, sizeof(float) * (size_t)Kcap * S) != cudaSuccess ||
+        ensure32(c, st->V32, n, S) != NM_OK || ensure32(c, st->Z32, n, S) != NM_OK) {
+      cudaGetLastError();
+      orth32 = false;
+    }
+  }
+  auto free32 = [&]() {
+    cudaFree(W32);
+    cudaFree(T32);
+    cudaFree(dH32);
+    W32 = T32 = dH32 = nullptr;
+  };
+  // FP32 copy of basis block starting at column K
+  auto shadow = [&](int K) {
+    if (!orth32) return;
+    if (ensure32(c, st->V32, n, K + S) != NM_OK || ensure32(c, st->Z32, n, K + S) != NM_OK) {
+      orth32 = false;  // keep the FP64 Gram-Schmidt from here on
+      return;
+    }
+    blk_d2f(V.col(K), V.ld, st->V32.col(K), st->V32.ld, n, S, s);
+    blk_d2f(Z.col(K), Z.ld, st->Z32.col(K), st->Z32.ld, n, S, s);
+  };
   // FP64 block B~^-1: col-major (ld ldw) in -> col-major out
   auto bsolve_blk = [&](const double* in, size_t ldin, double* out, size_t ldout) {
     blk_from_colmajor<double>(in, ldin, n, sin_, s);
@@ -364,6 +532,7 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
                     Z.col(0), (int)Z.ld));
   CB(c, cublasDtrsm(hb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, S, &one, dR, S,
                     V.col(0), (int)V.ld));
+  shadow(0);
   // ---- filter graph: zin -> yout (row-major, FP32 or FP64)
   cudaGraphExec_t gexec = nullptr;
   long long graph_nodes = 0;
@@ -396,6 +565,15 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   int* dInfo = nullptr;
   int lwork = 0;
   NM_CUDA(c, cudaMalloc(&dInfo, sizeof(int)));
+  // phase timers: filter (gather .. column-major result) and Gram-Schmidt
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  for (auto& e : ev) NM_CUDA(c, cudaEventCreate(&e));
+  double tf = 0.0, to = 0.0;
+  auto add_phase_times = [&]() {
+    float a = 0.f, b = 0.f;
+    if (cudaEventElapsedTime(&a, ev[0], ev[1]) == cudaSuccess) tf += 1e-3 * a;
+    if (cudaEventElapsedTime(&b, ev[1], ev[2]) == cudaSuccess) to += 1e-3 * b;
+  };
   auto build_T = [&](int nb, std::vector<double>& T) {
     const int K = nb * S;
     T.assign((size_t)K * K, 0.0);
@@ -442,6 +620,10 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
     return NM_OK;
   };
   auto fail = [&](int code) {
+    free32();
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    ev[0] = ev[1] = ev[2] = nullptr;
     if (gexec) cudaGraphExecDestroy(gexec);
     cleanup_small();
     cudaFree(dT);
@@ -453,6 +635,7 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   for (int j = 0; j < max_blocks; ++j) {
     const int K = (j + 1) * S;  // basis columns 0..K-1 hold blocks 0..j
     // W = F(Z_j)
+    NM_CUDA(c, cudaEventRecord(ev[0], s));
     if (mixed) blk_gather_cols<float>(Z, j * S, n, f32b.zin, s);
     else blk_gather_cols<double>(Z, j * S, n, f64b.zin, s);
     if (gexec) {
@@ -463,9 +646,11 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
     }
     c->n_amv += (long long)pol.deg * S;
     c->n_bsolve += (long long)pol.deg * S;
-    c->n_spmv += (long long)pol.deg * (c->chebB.deg + (c->fs ? 2 + c->chebAp.deg : 1));
+    c->n_spmv += (long long)pol.deg * (mixed ? mass_cheb<float>(c).deg + (c->fs ? 2 + ap_cheb<float>(c).deg : 1)
+                                             : c->chebB.deg + (c->fs ? 2 + c->chebAp.deg : 1));
     if (mixed) blk_to_colmajor<float>(f32b.yout, n, Wc, ldw, s);
     else blk_to_colmajor<double>(f64b.yout, n, Wc, ldw, s);
+    NM_CUDA(c, cudaEventRecord(ev[1], s));
     // W -= Z_{j-1} R_j^T
     if (j > 0) {
       NM_CUDA(c, cudaMemcpyAsync(dR, Rblk[j - 1].data(), sizeof(double) * S * S, cudaMemcpyHostToDevice, s));
@@ -483,7 +668,23 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
     NM_CUDA(c, cudaMemcpyAsync(dG, Aj.data(), sizeof(double) * S * S, cudaMemcpyHostToDevice, s));
     CB(c, cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, S, S, &mone, Z.col(j * S), (int)Z.ld, dG, S, &one, Wc, (int)ldw));
     // full block Gram-Schmidt, two classical passes: H = V^T W, W -= Z H
-    for (int pass = 0; pass < 2; ++pass) {
+    const float onef = 1.0f, zerof = 0.0f;
+    for (int pass = 0; orth32 && pass < 2; ++pass) {
+      blk_d2f(Wc, ldw, W32, n, n, S, s);
+      for (int c0 = 0; c0 < K; c0 += Basis::kChunk) {
+        const int w = std::min(Basis::kChunk, K - c0);
+        CB(c, cublasSgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, w, S, n, &onef, st->V32.col(c0), (int)st->V32.ld, W32, n,
+                          &zerof, dH32 + c0, Kcap));
+      }
+      for (int c0 = 0; c0 < K; c0 += Basis::kChunk) {
+        const int w = std::min(Basis::kChunk, K - c0);
+        const float beta = c0 == 0 ? 0.0f : 1.0f;
+        CB(c, cublasSgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, S, w, &onef, st->Z32.col(c0), (int)st->Z32.ld, dH32 + c0,
+                          Kcap, &beta, T32, n));
+      }
+      blk_sub_f32(Wc, ldw, T32, n, n, S, s);
+    }
+    for (int pass = 0; !orth32 && pass < 2; ++pass) {
       for (int c0 = 0; c0 < K; c0 += Basis::kChunk) {
         const int w = std::min(Basis::kChunk, K - c0);
         CB(c, cublasDgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, w, S, n, &one, V.col(c0), (int)V.ld, Wc, (int)ldw, &zero,
@@ -495,9 +696,11 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
                           (int)ldw));
       }
     }
+    NM_CUDA(c, cudaEventRecord(ev[2], s));
     // Vn = B~^-1 W;  R from the Cholesky of Vn^T W;  Z_{j+1} = W R^-1, V_{j+1} = Vn R^-1
     bsolve_blk(Wc, ldw, Vc, ldw);
     if ((rc = gram(Vc, ldw, Wc, ldw, Gh))) return fail(rc);
+    add_phase_times();  // gram() synchronised the stream
     nblk = j + 1;
     if (!chol_upper(Gh.data(), S, Rh)) {
       done = true;  // block breakdown: the Krylov space is exhausted
@@ -514,6 +717,7 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
                       S, Z.col(K), (int)Z.ld));
     CB(c, cublasDtrsm(hb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, S, &one, dR,
                       S, V.col(K), (int)V.ld));
+    shadow(K);
     // restricted-trace convergence test every 64 vectors, first after eight
     // block steps: a block Krylov space of degree < 8 has not yet lifted the
     // wanted Ritz values above the bar, so an empty Ritz set that early would
@@ -564,6 +768,8 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   *Uout = U;
   *ncout = nc;
   *steps_out = K;
+  if (t_filter) *t_filter = tf;
+  if (t_orth) *t_orth = to;
   return NM_OK;
 }
 
@@ -610,7 +816,7 @@ int rayleigh_ritz64(nm_ctx* c, double** Uio, int nc) {
     blk_from_colmajor<double>(Up + (size_t)j0 * n, n, n, sin_, s);
     if (c->fs) {
       blk_et<double, double>(st->ET64, sin_, x0, s);
-      blk_ap_cheb_persistent<double, double>(st->Ap64, c->chebAp, x0, y0, apw, c->bar, c->d_status, st->coop, s);
+      blk_ap_solve<double, double>(c, st->Ap64, x0, y0, apw);
     }
     blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sout, nullptr, nullptr, nullptr, ep, s);
     blk_to_colmajor<double>(sout, n, AU + (size_t)j0 * n, n, s);

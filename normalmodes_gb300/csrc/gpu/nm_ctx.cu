@@ -402,4 +402,14 @@ int nm_time_op(nm_ctx* c, int which, int reps, double* ms_per_op, double* bytes_
   return NM_OK;
 }
 
+// Test hook of the failure detection: a grid-barrier wait that can never
+// complete gives up after spin_limit polls; the host then reads the status
+// word and reports NM_ERR_TIMEOUT, as for a persistent Chebyshev kernel.
+int nm_test_barrier_timeout(nm_ctx* c, long long spin_limit) {
+  if (!c || spin_limit <= 0 || spin_limit > kSpinLimit) return c ? set_err(c, NM_ERR_ARG, "bad spin limit") : NM_ERR_ARG;
+  const int rc = barrier_timeout_probe(c, spin_limit);
+  if (rc != NM_OK) return rc;
+  return check_status(c);
+}
+
 }  // extern "C"

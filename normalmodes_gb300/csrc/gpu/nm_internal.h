@@ -175,6 +175,9 @@ void cheb_solve_persistent(const Sell<VT>& M, const ChebSetup& ch, const XT* b, 
 int coop_blocks_for_persistent();
 // Bring the sticky device status back (sync); returns NM_OK or NM_ERR_TIMEOUT.
 int check_status(nm_ctx* c);
+// Runs a one-block kernel whose grid-barrier wait can never complete and
+// must give up after spin_limit polls (test hook of the bounded waits).
+int barrier_timeout_probe(nm_ctx* c, long long spin_limit);
 int upload_cheb(nm_ctx* c, ChebSetup& ch);
 // w = A_s v (+ E_s y); epilogue modes
 struct FiltEpi {

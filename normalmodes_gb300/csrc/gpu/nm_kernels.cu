@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(kThreads)
 // arrives; the last arrival resets the counter and bumps the generation; the
 // others poll the generation with a spin limit.  Returns false (and sets
 // *status) if the wait gave up or another block already failed.
-__device__ __forceinline__ bool grid_barrier(GridBar* bar, unsigned nblocks, int* status) {
+__device__ __forceinline__ bool grid_barrier(GridBar* bar, unsigned nblocks, int* status,
+                                             long long spin_limit = kSpinLimit) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -140,7 +141,7 @@ __device__ __forceinline__ bool grid_barrier(GridBar* bar, unsigned nblocks, int
           ok = 0;
           break;
         }
-        if (++spins > kSpinLimit) {
+        if (++spins > spin_limit) {
           atomicExch(status, 1);
           ok = 0;
           break;
@@ -474,6 +475,23 @@ void cheb_solve_persistent(const Sell<VT>& M, const ChebSetup& ch, const XT* b, 
   cudaLaunchKernelEx(&cfg, k_cheb_persist<VT, XT>, v, b, x, r, xi, d0, d1, coef, deg, it, bar, status);
   NM_COUNT(1);
 }
+// Test hook for the bounded wait: one block waits at the grid barrier for
+// `phantom` blocks that are never launched, so the wait runs out after
+// `spin_limit` polls, the kernel sets the status word and returns.
+__global__ void k_barrier_probe(GridBar* bar, int* status, unsigned phantom, long long spin_limit) {
+  grid_barrier(bar, gridDim.x + phantom, status, spin_limit);
+}
+
+int barrier_timeout_probe(nm_ctx* c, long long spin_limit) {
+  NM_CUDA(c, cudaMemsetAsync(c->bar, 0, sizeof(GridBar), c->stream));
+  NM_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream));
+  k_barrier_probe<<<1, 32, 0, c->stream>>>(c->bar, c->d_status, 1u, spin_limit);
+  NM_COUNT(1);
+  NM_CUDA(c, cudaGetLastError());
+  NM_CUDA(c, cudaStreamSynchronize(c->stream));
+  return NM_OK;
+}
+
 template void cheb_solve_persistent<double, double>(const Sell<double>&, const ChebSetup&, const double*, double*,
                                                     double*, GridBar*, int*, int, cudaStream_t);
 template void cheb_solve_persistent<float, float>(const Sell<float>&, const ChebSetup&, const float*, float*, float*,

@@ -412,7 +412,8 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
   if (o.block > 1) {
     converged = true;
     int steps = 0;
-    if ((rc = block_lanczos(c, pol, maxit, o.use_graph != 0, &U, &nc, &steps))) return rc;
+    if ((rc = block_lanczos(c, pol, maxit, o.use_graph != 0, &U, &nc, &steps, &res->t_filter, &res->t_orth)))
+      return rc;
     // FP32 filter: close Ritz pairs are mixed at the FP32 noise level; an
     // FP64 Rayleigh-Ritz over the Ritz block separates them.
     if (mixed && (rc = rayleigh_ritz64(c, &U, nc))) {
@@ -603,6 +604,26 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
   }
   if (!converged && kdim >= maxit) return set_err(c, NM_ERR_NOCONV, "Lanczos reached MAXIT before convergence");
   return NM_OK;
+}
+
+int nm_solve_batched(nm_ctx* c, const nm_slice* slices, int nslices, const nm_solve_opts* opts, nm_result* results) {
+  if (!c) return NM_ERR_ARG;
+  if (!slices || !results || nslices < 0) return set_err(c, NM_ERR_ARG, "nm_solve_batched: bad arguments");
+  for (int i = 0; i < nslices; ++i) std::memset(&results[i], 0, sizeof(nm_result));
+  for (int i = 0; i < nslices; ++i) {
+    if (!(slices[i].f_hi_mhz > slices[i].f_lo_mhz) || !(slices[i].f_lo_mhz >= 0.0))
+      return set_err(c, NM_ERR_ARG, "nm_solve_batched: slice " + std::to_string(i) + " is not an interval");
+  }
+  int first_err = NM_OK;
+  for (int i = 0; i < nslices; ++i) {
+    const int rc = nm_solve(c, slices[i].f_lo_mhz, slices[i].f_hi_mhz, opts, &results[i]);
+    if (rc == NM_ERR_NOCONV) {
+      if (first_err == NM_OK) first_err = rc;
+      continue;  // the slice's result holds what converged; the others still run
+    }
+    if (rc != NM_OK) return rc;
+  }
+  return first_err;
 }
 
 }  // extern "C"

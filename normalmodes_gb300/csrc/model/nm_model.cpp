@@ -1375,6 +1375,27 @@ int nmm_mesh_arrays(const nmm_model* m, const double** xyz, const int** tets, co
   return NMM_OK;
 }
 
+int nmm_set_material(nmm_model* m, const double* vp, const double* vs, const double* rho) {
+  if (!m || !vp || !vs || !rho) return fail(NMM_ERR_ARG, "null argument");
+  const size_t len = (size_t)m->pnp * m->ntet;
+  // the solid / fluid split (and with it the DOF structure) must not change
+  for (int k = 0; k < m->ntet; ++k) {
+    double mx = 0.0, mxold = 0.0;
+    for (int l = 0; l < m->pnp; ++l) {
+      const size_t q = (size_t)m->pnp * k + l;
+      if (!(vp[q] > 0.0) || !(rho[q] > 0.0) || vs[q] < 0.0) return fail(NMM_ERR_ARG, "non-physical material");
+      mx = std::max(mx, rho[q] * vs[q] * vs[q]);
+      mxold = std::max(mxold, m->rho[q] * m->vs[q] * m->vs[q]);
+    }
+    if ((mx >= 1e-8) != (mxold >= 1e-8)) return fail(NMM_ERR_ARG, "material change would turn a solid element fluid or back");
+  }
+  m->vp.assign(vp, vp + len);
+  m->vs.assign(vs, vs + len);
+  m->rho.assign(rho, rho + len);
+  m->assembled = false;
+  return NMM_OK;
+}
+
 int nmm_reference(const nmm_model* m, const double** nodes_rst, const double** massm, const double** drst,
                   const double** massf, const int** fmask) {
   if (!m) return fail(NMM_ERR_ARG, "null model");

@@ -69,6 +69,7 @@ def lib() -> C.CDLL:
         L.nmm_element_matrices.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                            C.POINTER(C.c_int)]
         L.nmm_reference.argtypes = [vp] + [C.c_void_p] * 5
+        L.nmm_set_material.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.nmm_write_vector.argtypes = [C.c_char_p, C.POINTER(C.c_double), C.c_longlong]
         L.nmm_last_error.restype = C.c_char_p
         L.nmm_destroy.argtypes = [vp]
@@ -178,6 +179,14 @@ class Model:
             "vs": arr(ptrs[8], C.c_double, pnp * nt).reshape(nt, pnp),
             "rho": arr(ptrs[9], C.c_double, pnp * nt).reshape(nt, pnp),
         }
+
+    def set_material(self, vp, vs, rho, assemble: bool = True) -> None:
+        """Replace the per-element nodal material (ntet x pnp arrays) and
+        re-assemble; the solid / fluid split must not change."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (vp, vs, rho)]
+        _check(lib().nmm_set_material(self._h, *[a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs]))
+        if assemble:
+            self.assemble()
 
     def element_matrices(self, k: int):
         i = self.info()

@@ -30,7 +30,7 @@ EXPORTS = [
     "nm_create", "nm_destroy", "nm_default_opts", "nm_default_solve_opts", "nm_amv", "nm_bmv", "nm_bsolve",
     "nm_amv_dev", "nm_bmv_dev", "nm_bsolve_dev", "nm_amv_block", "nm_bmv_block", "nm_bsolve_block", "nm_solve",
     "nm_result_free", "nm_get_info", "nm_get_stream", "nm_last_error", "nm_sync", "nm_time_op",
-    "nm_bsolve_dev_noalloc",
+    "nm_bsolve_dev_noalloc", "nm_adjoint", "nm_solve_batched",
 ]
 
 
@@ -59,7 +59,22 @@ class NmResult(C.Structure):
                 ("t_bounds", C.c_double), ("t_filter_design", C.c_double), ("t_lanczos", C.c_double),
                 ("t_ritz", C.c_double), ("t_total", C.c_double),
                 ("n_amv", C.c_longlong), ("n_bsolve", C.c_longlong), ("n_spmv", C.c_longlong),
-                ("n_kernels", C.c_longlong)]
+                ("n_kernels", C.c_longlong), ("t_filter", C.c_double), ("t_orth", C.c_double)]
+
+
+class NmElemModel(C.Structure):
+    _fields_ = [("ntet", C.c_int), ("pnp", C.c_int), ("nnode", C.c_int), ("fluid_solid", C.c_int),
+                ("tets", C.c_void_p), ("xyz", C.c_void_p), ("fluid", C.c_void_p), ("vstt", C.c_void_p),
+                ("rnum", C.c_void_p), ("pstt", C.c_void_p), ("vp", C.c_void_p), ("vs", C.c_void_p),
+                ("rho", C.c_void_p), ("ref_mass", C.c_void_p), ("ref_drst", C.c_void_p)]
+
+
+class NmSlice(C.Structure):
+    _fields_ = [("f_lo_mhz", C.c_double), ("f_hi_mhz", C.c_double)]
+
+
+NM_ADJ_PAIR = 0
+NM_ADJ_MULTIPLET = 1
 
 
 class NmInfo(C.Structure):
@@ -104,6 +119,10 @@ def lib() -> C.CDLL:
         L.nm_last_error.restype = C.c_char_p
         L.nm_sync.argtypes = [vp]
         L.nm_time_op.argtypes = [vp, C.c_int, C.c_int, dp, dp, C.POINTER(C.c_int)]
+        L.nm_test_barrier_timeout.argtypes = [vp, C.c_longlong]
+        L.nm_solve_batched.argtypes = [vp, C.POINTER(NmSlice), C.c_int, C.POINTER(NmSolveOpts), C.POINTER(NmResult)]
+        L.nm_adjoint.argtypes = [vp, C.POINTER(NmElemModel), C.c_int, dp, dp, C.c_int, C.c_int, C.c_double, dp,
+                                 C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.nm_test_find_pol.argtypes = [dp, C.c_double, C.c_double, C.c_int, dp, C.c_int, dp]
         L.nm_test_tridiag.argtypes = [dp, dp, C.c_int, C.c_double, C.c_double, dp, dp, C.c_int]
         L.nm_test_sell.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), dp,
@@ -228,12 +247,11 @@ class Solver:
         self._check(lib().nm_time_op(self._h, which, reps, C.byref(ms), C.byref(by), C.byref(la)))
         return ms.value, by.value, la.value
 
-    def solve(self, lowfreq: float, upfreq: float, maxit: int = 0, tol: float = 0.0, ab_bounds=None,
-              want_vectors: bool = True, unscale: bool = False, use_graph: bool = True, damping: int = 1,
-              mlan_bounds: int = 0, allow_noconv: bool = False, block: int = 0) -> SolveResult:
-        L = lib()
+    @staticmethod
+    def _solve_opts(maxit=0, tol=0.0, ab_bounds=None, want_vectors=True, unscale=False, use_graph=True, damping=1,
+                    mlan_bounds=0, block=0) -> "NmSolveOpts":
         o = NmSolveOpts()
-        L.nm_default_solve_opts(C.byref(o))
+        lib().nm_default_solve_opts(C.byref(o))
         o.maxit = maxit
         o.tol = tol
         o.want_vectors = int(want_vectors)
@@ -244,24 +262,83 @@ class Solver:
         o.block = block
         if ab_bounds is not None:
             o.ab_bounds[0], o.ab_bounds[1] = ab_bounds
+        return o
+
+    @staticmethod
+    def _result(r: "NmResult", want_vectors: bool) -> SolveResult:
+        nev, n = r.nev, r.n
+        arr = lambda p: np.ctypeslib.as_array(p, shape=(max(nev, 1),))[:nev].copy() if nev else np.zeros(0)
+        vec = None
+        if want_vectors and nev:
+            vec = np.ctypeslib.as_array(r.vec, shape=(nev * n,)).reshape(nev, n).T.copy()
+        return SolveResult(arr(r.lam), vec, arr(r.err_ref), arr(r.res2), tuple(r.xintv), r.pol_deg, r.pol_gam,
+                           r.pol_bar, r.lanczos_steps, r.nritz_above_bar,
+                           {"bounds": r.t_bounds, "filter_design": r.t_filter_design, "lanczos": r.t_lanczos,
+                            "ritz": r.t_ritz, "total": r.t_total, "filter": r.t_filter, "orth": r.t_orth},
+                           {"amv": r.n_amv, "bsolve": r.n_bsolve, "spmv": r.n_spmv, "kernels": r.n_kernels})
+
+    def solve(self, lowfreq: float, upfreq: float, maxit: int = 0, tol: float = 0.0, ab_bounds=None,
+              want_vectors: bool = True, unscale: bool = False, use_graph: bool = True, damping: int = 1,
+              mlan_bounds: int = 0, allow_noconv: bool = False, block: int = 0) -> SolveResult:
+        L = lib()
+        o = self._solve_opts(maxit, tol, ab_bounds, want_vectors, unscale, use_graph, damping, mlan_bounds, block)
         r = NmResult()
         rc = L.nm_solve(self._h, lowfreq, upfreq, C.byref(o), C.byref(r))
-        if rc != 0 and not (allow_noconv and rc == -4):
-            L.nm_result_free(C.byref(r))
-            self._check(rc)
         try:
-            nev, n = r.nev, r.n
-            arr = lambda p: np.ctypeslib.as_array(p, shape=(max(nev, 1),))[:nev].copy() if nev else np.zeros(0)
-            vec = None
-            if want_vectors and nev:
-                vec = np.ctypeslib.as_array(r.vec, shape=(nev * n,)).reshape(nev, n).T.copy()
-            return SolveResult(arr(r.lam), vec, arr(r.err_ref), arr(r.res2), tuple(r.xintv), r.pol_deg, r.pol_gam,
-                               r.pol_bar, r.lanczos_steps, r.nritz_above_bar,
-                               {"bounds": r.t_bounds, "filter_design": r.t_filter_design, "lanczos": r.t_lanczos,
-                                "ritz": r.t_ritz, "total": r.t_total},
-                               {"amv": r.n_amv, "bsolve": r.n_bsolve, "spmv": r.n_spmv, "kernels": r.n_kernels})
+            if rc != 0 and not (allow_noconv and rc == -4):
+                self._check(rc)
+            return self._result(r, want_vectors)
         finally:
             L.nm_result_free(C.byref(r))
+
+    def solve_batched(self, slices, allow_noconv: bool = False, **kw) -> list:
+        """nm_solve_batched over [(f_lo, f_hi), ...] mHz; one SolveResult per
+        slice.  Keyword options as for solve()."""
+        L = lib()
+        want = kw.get("want_vectors", True)
+        o = self._solve_opts(**kw)
+        arr = (NmSlice * len(slices))(*[NmSlice(lo, hi) for lo, hi in slices])
+        res = (NmResult * len(slices))()
+        rc = L.nm_solve_batched(self._h, arr, len(slices), C.byref(o), res)
+        try:
+            if rc != 0 and not (allow_noconv and rc == -4):
+                self._check(rc)
+            return [self._result(res[i], want) for i in range(len(slices))]
+        finally:
+            for i in range(len(slices)):
+                L.nm_result_free(C.byref(res[i]))
+
+    def adjoint(self, mesh: dict, ref: dict, lam, X, mode: int = NM_ADJ_PAIR, tol: float = 1e-6):
+        """Per-element sensitivities (rho, kappa, mu) of the eigenvalues `lam`
+        with unscaled, B-normalised eigenvectors X (n x k), through
+        nm_adjoint.  `mesh` is Model.mesh(), `ref` Model.reference().
+        Returns (grad[k or ngroups, ntet, 3], group[k])."""
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        X = np.asfortranarray(X, dtype=np.float64)
+        k = lam.size
+        nt, pnp = mesh["tets"].shape
+        keep = {
+            "tets": np.ascontiguousarray(mesh["tets"], dtype=np.int32),
+            "xyz": np.ascontiguousarray(mesh["xyz"], dtype=np.float64),
+            "fluid": np.ascontiguousarray(mesh["fluid"], dtype=np.uint8),
+            "vstt": np.ascontiguousarray(mesh["vstt"], dtype=np.int32),
+            "rnum": np.ascontiguousarray(mesh["rnum"], dtype=np.int32),
+            "pstt": np.ascontiguousarray(mesh["pstt"], dtype=np.int32),
+            "vp": np.ascontiguousarray(mesh["vp"], dtype=np.float64),
+            "vs": np.ascontiguousarray(mesh["vs"], dtype=np.float64),
+            "rho": np.ascontiguousarray(mesh["rho"], dtype=np.float64),
+            "M": np.ascontiguousarray(ref["M"], dtype=np.float64),
+            "D": np.ascontiguousarray(ref["Drst"], dtype=np.float64),
+        }
+        em = NmElemModel(nt, pnp, mesh["xyz"].shape[0], int(self.info().fs),
+                         *[keep[q].ctypes.data for q in ("tets", "xyz", "fluid", "vstt", "rnum", "pstt", "vp", "vs",
+                                                         "rho", "M", "D")])
+        grad = np.zeros((k, nt, 3))
+        group = np.zeros(k, dtype=np.int32)
+        ng = C.c_int()
+        self._check(lib().nm_adjoint(self._h, C.byref(em), k, _dp(lam), _dp(X), X.shape[0], mode, tol, _dp(grad),
+                                     group.ctypes.data_as(C.POINTER(C.c_int)), C.byref(ng)))
+        return grad[: ng.value], group
 
     def close(self):
         if self._h:

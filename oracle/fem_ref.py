@@ -111,6 +111,33 @@ def geometry(R, mesh, k):
     return invJ, detJ
 
 
+def solid_stiffness(R, D, detJ, lam, mu):
+    """Solid element stiffness for nodal Lame lambda / mu (the TM of
+    CGE3D_ISO, src/mod_cg_create_matrix.f90:1043-1219)."""
+    p = R["pnp"]
+    M = R["M"]
+    Ml = M @ np.diag(lam)
+    Ml = (Ml + Ml.T) / 2
+    Mm = M @ np.diag(mu)
+    Mm = (Mm + Mm.T) / 2
+    OP1 = [Ml @ D[i] for i in range(3)]
+    OP2 = [Mm @ D[i] for i in range(3)]
+    OPt = [D[i].T @ OP2[i] for i in range(3)]
+    OPs = OPt[0] + OPt[1] + OPt[2]
+    TM = np.zeros((3 * p, 3 * p))
+    for i in range(3):
+        for j in range(3):
+            if i == j:
+                O = OPs + OPt[i] + D[i].T @ OP1[i]
+                O = (O + O.T) / 2
+            else:
+                tmp = D[i].T @ OP1[j] + D[j].T @ OP2[i]
+                trs = D[j].T @ OP1[i] + D[i].T @ OP2[j]
+                O = (trs.T + tmp) / 2
+            TM[i * p:(i + 1) * p, j * p:(j + 1) * p] = O * detJ
+    return TM
+
+
 def element_matrices(R, mesh, k, fluid_solid: bool):
     p = R["pnp"]
     M = R["M"]
