@@ -97,6 +97,7 @@ typedef struct {
   long long n_kernels;   /* kernels of this library launched by the solve            */
   double t_filter;       /* block path: seconds in the filter applications (CUDA events) */
   double t_orth;         /* block path: seconds in the block Gram-Schmidt (CUDA events)  */
+  double t_eig;          /* block path: seconds in the projected (block-tridiagonal) eigensolves */
 } nm_result;
 
 typedef struct nm_ctx nm_ctx;

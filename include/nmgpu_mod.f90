@@ -44,7 +44,7 @@ module nmgpu_mod
     integer(c_int) :: lanczos_steps, nritz_above_bar
     real(c_double) :: t_bounds, t_filter_design, t_lanczos, t_ritz, t_total
     integer(c_long_long) :: n_amv, n_bsolve, n_spmv, n_kernels
-    real(c_double) :: t_filter, t_orth
+    real(c_double) :: t_filter, t_orth, t_eig
   end type nm_result
 
   interface

@@ -124,6 +124,23 @@ int nmm_reference(const nmm_model* m, const double** nodes_rst, const double** m
  * (src/mod_pevsl.f90:188-201,225-247): raw float64 per vector. */
 int nmm_write_vector(const char* path, const double* x, long long n);
 
+/* The reference's result files (src/mod_pevsl.f90:188-247, names of
+ * src/mod_para.f90:269-288):
+ *   <outputdir><basename>_JOB<job>_pod<p>_np<nproc>_<low>_<up>_<i>.dat
+ *       eigenvector i (1-based), raw float64, n values in DOF order;
+ *   <outputdir><basename>_pod<p>_np<nproc>_vlist.dat
+ *       int32 per node in DOF order: its 1-based id in the input numbering
+ *       (vertices of _node.dat, then P2 edge nodes);
+ *   <outputdir><basename>_pod<p>_np<nproc>_vstat.dat (fluid-solid models)
+ *       int32 node status (vstat codes 0..5).
+ * <low>/<up> are the frequencies as the reference writes REAL(4) values
+ * (gfortran list-directed).  X is n x nev column-major with leading
+ * dimension ldx (unscaled eigenvectors).  The eigenvector file prefix is
+ * copied to prefix_out (may be NULL). */
+int nmm_write_results(const nmm_model* m, const char* outputdir, const char* basename, int job, int nproc,
+                      double lowfreq, double upfreq, int nev, const double* X, long long ldx, char* prefix_out,
+                      int prefix_len);
+
 const char* nmm_last_error(void);
 void nmm_destroy(nmm_model* m);
 

@@ -1,0 +1,63 @@
+"""Mixed precision against FP64 on one spectrum slice.
+
+    python -m normalmodes_gb300.compare [--cells 24] [--porder 2] [--lateral 0.02]
+                                        [--interval 0.1 1.0] [--fp64-block 32|0]
+
+Solves the interval twice on one GPU: the mixed path (FP32 filter SpMMs,
+FP64 Lanczos and Rayleigh-Ritz, block of 32) and the FP64 path (block of 32,
+or the single-vector ChebLanNr with --fp64-block 0).  Prints one JSON line:
+both counts, the per-eigenpair relative eigenvalue difference
+|lam_mixed - lam_fp64| / |lam_fp64| (max, median, and the full list), both
+residual norms of both paths, and both solve times with their ratio.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+
+def main(argv=None) -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--cells", type=int, default=24)
+    ap.add_argument("--porder", type=int, default=2)
+    ap.add_argument("--lateral", type=float, default=0.02)
+    ap.add_argument("--interval", type=float, nargs=2, default=(0.1, 1.0))
+    ap.add_argument("--fp64-block", type=int, default=32)
+    a = ap.parse_args(argv)
+    from normalmodes_gb300.model import Model
+    from normalmodes_gb300.nmgpu import NM_PREC_FP64, NM_PREC_MIXED, Solver
+    kw = dict(n_cells=a.cells, porder=a.porder)
+    if a.lateral > 0:
+        kw.update(lateral_pert=a.lateral, lateral_lmax=8)
+    mats = Model.ball(**kw).operators()
+    lo, hi = a.interval
+    out = {"cells": a.cells, "porder": a.porder, "lateral": a.lateral, "interval_mhz": [lo, hi]}
+    res = {}
+    for name, prec, block in (("mixed", NM_PREC_MIXED, 32), ("fp64", NM_PREC_FP64, a.fp64_block)):
+        with Solver(mats, a.porder, precision=prec) as sv:
+            t = time.perf_counter()
+            r = sv.solve(lo, hi, block=block, want_vectors=False)
+            dt = time.perf_counter() - t
+        res[name] = r
+        out[name] = {"nev": len(r.lam), "seconds": round(dt, 3), "block": block, "lanczos_vectors": r.lanczos_steps,
+                     "filter_degree": r.pol_deg,
+                     "err_ref_max": float(r.err_ref.max()) if len(r.lam) else None,
+                     "err_ref_median": float(np.median(r.err_ref)) if len(r.lam) else None,
+                     "res2_max": float(r.res2.max()) if len(r.lam) else None,
+                     "res2_median": float(np.median(r.res2)) if len(r.lam) else None}
+    m, f = res["mixed"].lam, res["fp64"].lam
+    out["same_count"] = len(m) == len(f)
+    if len(m) == len(f) and len(f):
+        rel = np.abs(m - f) / np.abs(f)
+        out["eig_rel_diff_max"] = float(rel.max())
+        out["eig_rel_diff_median"] = float(np.median(rel))
+        out["eig_rel_diff"] = [float(x) for x in rel]
+    out["speedup_mixed_over_fp64"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -291,29 +291,28 @@ __device__ __forceinline__ XT ld(const XT* p) {
 // between them and can be in flight together.  CTAs take consecutive rows;
 // rows are numbered along a space-filling curve, so the rows in flight at
 // any time form a compact piece of the mesh whose neighbour rows stay in L2.
-// LATE: the own-row state is read after the gathers instead of before, and
-// registers are capped for full occupancy (more rows in flight per SM
-// instead of more loads in flight per row).
-template <typename VT, typename XT, int NC, int MODE, bool LATE = false>
-__global__ void __launch_bounds__(kT, LATE ? 8 : 1)
+template <typename VT, typename XT, int NC, int MODE, int UNR = 4>
+__global__ void __launch_bounds__(kT)
     k_mass_cheb(int ng, const int* __restrict__ rp, const int* __restrict__ ci, const VT* __restrict__ mv,
                 const XT* __restrict__ b, const XT* __restrict__ xcur, const XT* xprev, XT* xout, XT a, XT c,
-                XT inv_theta) {
+                XT inv_theta, int rpw) {
   const int lane = threadIdx.x & (kBlk - 1);
-  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int wpc = blockDim.x >> 5;  // warps per CTA
+  // the CTA owns wpc * rpw consecutive rows; its warps take them wpc at a
+  // time, so the rows in flight stay adjacent and the window slides
+  for (int r = 0; r < rpw; ++r) {
+  const int g = (blockIdx.x * rpw + r) * wpc + (threadIdx.x >> 5);
   if (g >= ng) return;
   const XT* src = MODE == 0 ? b : xcur;
   XT bo[NC], xc[NC], xp[NC];
   const size_t i0 = (size_t)NC * g * kBlk + lane;
-  auto load_own = [&]() {
+  // own-row state, loaded before the gathers so the loads overlap
 #pragma unroll
-    for (int p = 0; p < NC; ++p) {
-      bo[p] = b[i0 + p * kBlk];
-      xc[p] = MODE == 0 ? bo[p] * inv_theta : xcur[i0 + p * kBlk];
-      xp[p] = MODE == 0 ? (XT)0 : MODE == 1 ? bo[p] * inv_theta : xprev[i0 + p * kBlk];
-    }
-  };
-  if (!LATE) load_own();  // issued before the gathers so the loads overlap
+  for (int p = 0; p < NC; ++p) {
+    bo[p] = b[i0 + p * kBlk];
+    xc[p] = MODE == 0 ? bo[p] * inv_theta : xcur[i0 + p * kBlk];
+    xp[p] = MODE == 0 ? (XT)0 : MODE == 1 ? bo[p] * inv_theta : xprev[i0 + p * kBlk];
+  }
   XT t[NC];
 #pragma unroll
   for (int p = 0; p < NC; ++p) t[p] = 0;
@@ -323,21 +322,21 @@ __global__ void __launch_bounds__(kT, LATE ? 8 : 1)
     const int myh = lane < cnt ? __ldg(ci + base + lane) : 0;
     const XT mym = lane < cnt ? (XT)__ldg(mv + base + lane) : (XT)0;
     int k = 0;
-    for (; k + 4 <= cnt; k += 4) {
-      const XT* xs[4];
-      XT m[4];
+    for (; k + UNR <= cnt; k += UNR) {
+      const XT* xs[UNR];
+      XT m[UNR];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < UNR; ++u) {
         xs[u] = src + (size_t)NC * __shfl_sync(0xffffffffu, myh, k + u) * kBlk + lane;
         m[u] = __shfl_sync(0xffffffffu, mym, k + u);
       }
-      XT v[4][NC];
+      XT v[UNR][NC];
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+      for (int u = 0; u < UNR; ++u)
 #pragma unroll
         for (int p = 0; p < NC; ++p) v[u][p] = __ldg(xs[u] + p * kBlk);
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+      for (int u = 0; u < UNR; ++u)
 #pragma unroll
         for (int p = 0; p < NC; ++p) t[p] = fm<XT>(m[u], v[u][p], t[p]);
     }
@@ -348,12 +347,12 @@ __global__ void __launch_bounds__(kT, LATE ? 8 : 1)
       for (int p = 0; p < NC; ++p) t[p] = fm<XT>(m, __ldg(xs + p * kBlk), t[p]);
     }
   }
-  if (LATE) load_own();
 #pragma unroll
   for (int p = 0; p < NC; ++p) {
     const XT tt = MODE == 0 ? t[p] * inv_theta : t[p];
     // x_{j+1} = x_j + a (x_j - x_{j-1}) + c (b - M x_j)
     xout[i0 + p * kBlk] = fm<XT>(c, bo[p] - tt, fm<XT>(a, xc[p] - xp[p], xc[p]));
+  }
   }
 }
 
@@ -893,14 +892,24 @@ bool gather_vec(int nc) {
   return v < 0 ? nc == 1 : v != 0;
 }
 
-// Register-capped late-load variant of k_mass_cheb (NM_MASS_LATE=1).
-bool gather_late() {
-  static int v = -1;
-  if (v < 0) {
-    v = 0;
-    if (const char* e = std::getenv("NM_MASS_LATE")) v = std::atoi(e) != 0;
+// Rows each warp of k_mass_cheb takes in turn (NM_GATHER_RPW, 1..16).
+int gather_rpw() {
+  static int v = 0;
+  if (!v) {
+    v = 1;
+    if (const char* e = std::getenv("NM_GATHER_RPW")) v = std::min(16, std::max(1, std::atoi(e)));
   }
-  return v != 0;
+  return v;
+}
+
+// Gathers in flight per warp in k_mass_cheb (4 or 8; NM_GATHER_UNROLL).
+int gather_unroll() {
+  static int v = 0;
+  if (!v) {
+    v = 4;
+    if (const char* e = std::getenv("NM_GATHER_UNROLL")) v = std::atoi(e) == 8 ? 8 : 4;
+  }
+  return v;
 }
 
 template <typename VT, typename XT, int NC>
@@ -911,30 +920,33 @@ void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT*
   XT* buf[2] = {work, work + len};  // x_j lives in buf[j & 1]
   const XT it = (XT)ch.inv_theta;
   const int thr = gather_threads(), rows = thr / 32;
+  const int rpw = NC == 3 ? gather_rpw() : 1;  // rows per warp of k_mass_cheb
   const int grid = (ng + rows - 1) / rows;
+  const int grid_m = (ng + rows * rpw - 1) / (rows * rpw);
   for (int j = 1; j <= ch.deg; ++j) {
     const XT a = (XT)ch.a[j - 1], c = (XT)ch.c[j - 1];
     XT* out = j == ch.deg ? x : buf[(j + 1) & 1];
     const XT* cur = buf[j & 1];
     const XT* prev = buf[(j + 1) & 1];
-#define NM_MC(K, MODE) K<VT, XT, NC, MODE><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it)
+#define NM_MV(MODE) \
+  k_gcheb<VT, XT, NC, MODE><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it)
+#define NM_MC(MODE, U) \
+  k_mass_cheb<VT, XT, NC, MODE, U><<<grid_m, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it, rpw)
     if (gather_vec(NC)) {
-      if (j == 1) NM_MC(k_gcheb, 0);
-      else if (j == 2) NM_MC(k_gcheb, 1);
-      else NM_MC(k_gcheb, 2);
-    } else if (gather_late()) {
-#define NM_ML(MODE) \
-  k_mass_cheb<VT, XT, NC, MODE, true><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it)
-      if (j == 1) NM_ML(0);
-      else if (j == 2) NM_ML(1);
-      else NM_ML(2);
-#undef NM_ML
+      if (j == 1) NM_MV(0);
+      else if (j == 2) NM_MV(1);
+      else NM_MV(2);
+    } else if (gather_unroll() == 8) {
+      if (j == 1) NM_MC(0, 8);
+      else if (j == 2) NM_MC(1, 8);
+      else NM_MC(2, 8);
     } else {
-      if (j == 1) NM_MC(k_mass_cheb, 0);
-      else if (j == 2) NM_MC(k_mass_cheb, 1);
-      else NM_MC(k_mass_cheb, 2);
+      if (j == 1) NM_MC(0, 4);
+      else if (j == 2) NM_MC(1, 4);
+      else NM_MC(2, 4);
     }
 #undef NM_MC
+#undef NM_MV
     nmg::add_launches(1);
   }
 }
@@ -1104,6 +1116,13 @@ __global__ void k_d2f(const double* __restrict__ src, size_t lds, float* __restr
   const int c = (int)(t / n), i = (int)(t % n);
   dst[(size_t)c * ldd + i] = (float)src[(size_t)c * lds + i];
 }
+__global__ void k_f2d(const float* __restrict__ src, size_t lds, double* __restrict__ dst, size_t ldd, int n,
+                      int cols) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * cols) return;
+  const int c = (int)(t / n), i = (int)(t % n);
+  dst[(size_t)c * ldd + i] = (double)src[(size_t)c * lds + i];
+}
 __global__ void k_sub_f32(double* __restrict__ W, size_t ldw, const float* __restrict__ T, size_t ldt, int n,
                           int cols) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1116,6 +1135,11 @@ __global__ void k_sub_f32(double* __restrict__ W, size_t ldw, const float* __res
 void blk_d2f(const double* src, size_t lds, float* dst, size_t ldd, int n, int cols, cudaStream_t s) {
   const long long tot = (long long)n * cols;
   k_d2f<<<(int)((tot + 255) / 256), 256, 0, s>>>(src, lds, dst, ldd, n, cols);
+  nmg::add_launches(1);
+}
+void blk_f2d(const float* src, size_t lds, double* dst, size_t ldd, int n, int cols, cudaStream_t s) {
+  const long long tot = (long long)n * cols;
+  k_f2d<<<(int)((tot + 255) / 256), 256, 0, s>>>(src, lds, dst, ldd, n, cols);
   nmg::add_launches(1);
 }
 void blk_sub_f32(double* W, size_t ldw, const float* T, size_t ldt, int n, int cols, cudaStream_t s) {

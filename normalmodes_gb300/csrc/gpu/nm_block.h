@@ -134,6 +134,7 @@ struct Basis32 {
 // Column-major conversions of S-column blocks: dst = (float)src; W -= T.
 void blk_d2f(const double* src, size_t lds, float* dst, size_t ldd, int n, int cols, cudaStream_t s);
 void blk_sub_f32(double* W, size_t ldw, const float* T, size_t ldt, int n, int cols, cudaStream_t s);
+void blk_f2d(const float* src, size_t lds, double* dst, size_t ldd, int n, int cols, cudaStream_t s);
 
 // Grouped operators and buffers of the batched path.
 struct BlockState {
@@ -160,7 +161,7 @@ void block_free(nm_ctx* c);
 // Block filtered Lanczos; on success U (n x nc, column-major, device, owned
 // by the caller) holds the Ritz vectors with p(theta) >= bar.
 int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double** U, int* nc, int* steps,
-                  double* t_filter, double* t_orth);
+                  double* t_filter, double* t_orth, double* t_eig);
 // FP64 Rayleigh-Ritz on the columns of U (n x nc): U <- U Q with
 // (U^T A U) Q = (U^T B U) Q Theta.  Resolves the mixing of close Ritz pairs
 // left by an FP32 filter.

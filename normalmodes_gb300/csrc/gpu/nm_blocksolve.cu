@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -424,7 +425,7 @@ int ensure32(nm_ctx* c, Basis32& b, int n, int ncols) {
 }  // namespace
 
 int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double** Uout, int* ncout, int* steps_out,
-                  double* t_filter, double* t_orth) {
+                  double* t_filter, double* t_orth, double* t_eig) {
   BlockState* st = bs(c);
   if (!st || !st->ok) return set_err(c, NM_ERR_ARG, "block mode needs the 3-component operator structure");
   const int n = c->n, np = c->np, S = kBlk;
@@ -592,7 +593,14 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   };
   // eigen-decomposition of T on the device; vectors if want_vec
   std::vector<double> evals;
+  double teig = 0.0;
   auto eig_T = [&](int nb, bool want_vec) -> int {
+    const auto t_start = std::chrono::steady_clock::now();
+    struct Acc {
+      double& t;
+      std::chrono::steady_clock::time_point t0;
+      ~Acc() { t += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+    } acc{teig, t_start};
     const int K = nb * S;
     std::vector<double> T;
     build_T(nb, T);
@@ -718,11 +726,13 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
     CB(c, cublasDtrsm(hb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, S, &one, dR,
                       S, V.col(K), (int)V.ld));
     shadow(K);
-    // restricted-trace convergence test every 64 vectors, first after eight
-    // block steps: a block Krylov space of degree < 8 has not yet lifted the
-    // wanted Ritz values above the bar, so an empty Ritz set that early would
-    // end the solve through the "no eigenvalue in the interval" exit.
-    if (K < 50 || j < 7 || ((K / S) % 2) != 0) continue;
+    // restricted-trace convergence test every 64 vectors (every 128 from
+    // 2048 on, where the dense eigensolve of T costs more than the block
+    // steps it could save), first after eight block steps: a block Krylov
+    // space of degree < 8 has not yet lifted the wanted Ritz values above the
+    // bar, so an empty Ritz set that early would end the solve through the
+    // "no eigenvalue in the interval" exit.
+    if (K < 50 || j < 7 || ((K / S) % 2) != 0 || (K >= 2048 && (K / S) % 4 != 0)) continue;
     if ((rc = eig_T(nblk, false))) return fail(rc);
     double tr1 = 0.0;
     int cnt = 0;
@@ -757,11 +767,33 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   if (nc > 0) {
     NM_CUDA(c, cudaMalloc(&U, sizeof(double) * (size_t)n * nc));
     const double* Ssel = dT + (size_t)first * K;  // eigenvectors first..K-1, ld = K
-    for (int c0 = 0; c0 < K; c0 += Basis::kChunk) {
-      const int w = std::min(Basis::kChunk, K - c0);
-      const double beta = c0 == 0 ? 0.0 : 1.0;
-      CB(c, cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, nc, w, &one, V.col(c0), (int)V.ld, Ssel + c0, K, &beta, U, n));
+    float *U32 = nullptr, *S32 = nullptr;
+    if (orth32 && cudaMalloc(&U32, sizeof(float) * (size_t)n * nc) == cudaSuccess &&
+        cudaMalloc(&S32, sizeof(float) * (size_t)K * nc) == cudaSuccess) {
+      // mixed path: U = V S from the FP32 basis copy (the span carries FP32
+      // rounding from the filter already; the FP64 Rayleigh-Ritz that
+      // follows sets the eigenpairs)
+      const float onef = 1.0f;
+      blk_d2f(Ssel, K, S32, K, K, nc, s);
+      for (int c0 = 0; c0 < K; c0 += Basis::kChunk) {
+        const int w = std::min(Basis::kChunk, K - c0);
+        const float beta = c0 == 0 ? 0.0f : 1.0f;
+        CB(c, cublasSgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, nc, w, &onef, st->V32.col(c0), (int)st->V32.ld, S32 + c0,
+                          K, &beta, U32, n));
+      }
+      blk_f2d(U32, n, U, n, n, nc, s);
+      NM_CUDA(c, cudaStreamSynchronize(s));
+    } else {
+      cudaGetLastError();
+      for (int c0 = 0; c0 < K; c0 += Basis::kChunk) {
+        const int w = std::min(Basis::kChunk, K - c0);
+        const double beta = c0 == 0 ? 0.0 : 1.0;
+        CB(c, cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, nc, w, &one, V.col(c0), (int)V.ld, Ssel + c0, K, &beta, U,
+                          n));
+      }
     }
+    cudaFree(U32);
+    cudaFree(S32);
   }
   NM_CUDA(c, cudaStreamSynchronize(s));
   fail(NM_OK);  // releases the scratch (T, workspace, small matrices)
@@ -770,6 +802,7 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   *steps_out = K;
   if (t_filter) *t_filter = tf;
   if (t_orth) *t_orth = to;
+  if (t_eig) *t_eig = teig;
   return NM_OK;
 }
 

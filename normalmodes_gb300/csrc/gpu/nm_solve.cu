@@ -412,7 +412,8 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
   if (o.block > 1) {
     converged = true;
     int steps = 0;
-    if ((rc = block_lanczos(c, pol, maxit, o.use_graph != 0, &U, &nc, &steps, &res->t_filter, &res->t_orth)))
+    if ((rc = block_lanczos(c, pol, maxit, o.use_graph != 0, &U, &nc, &steps, &res->t_filter, &res->t_orth,
+                            &res->t_eig)))
       return rc;
     // FP32 filter: close Ritz pairs are mixed at the FP32 noise level; an
     // FP64 Rayleigh-Ritz over the Ritz block separates them.

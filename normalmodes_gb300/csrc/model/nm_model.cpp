@@ -377,6 +377,7 @@ struct nmm_model {
   std::vector<unsigned char> fluid;  // ntet
   std::vector<unsigned char> bface;  // 4*ntet: face on the outer boundary
   std::vector<int> vstat, rnum, pnum, vstt, pstt;
+  std::vector<int> orig;  // per node: its id in the input numbering (vertices, then edge nodes)
   int n = 0, np = 0;
   bool fsexist = false, purefluid = false, assembled = false;
   int n_cout4 = 0;
@@ -574,6 +575,9 @@ void renumber_morton(nmm_model* m, const std::vector<std::array<int, 3>>& gv) {
   std::sort(key.begin(), key.end());
   std::vector<int> newid(m->nnode);
   for (int r = 0; r < m->nnode; ++r) newid[key[r].second] = r;
+  std::vector<int> orig(m->nnode);
+  for (int i = 0; i < m->nnode; ++i) orig[newid[i]] = m->orig[i];
+  m->orig.swap(orig);
   std::vector<double> xyz(m->xyz.size());
   for (int i = 0; i < m->nnode; ++i)
     for (int c = 0; c < 3; ++c) xyz[3 * (size_t)newid[i] + c] = m->xyz[3 * (size_t)i + c];
@@ -589,6 +593,8 @@ void finish_mesh(nmm_model* m, const std::vector<int>& tv, const std::vector<std
     m->tet = tv;
   }
   mark_boundary_faces(m, tv);
+  m->orig.resize(m->nnode);
+  for (int i = 0; i < m->nnode; ++i) m->orig[i] = i;
   if (grid) {
     std::vector<std::array<int, 3>> gv(m->nnode, {0, 0, 0});
     for (int i = 0; i < m->nvert; ++i) gv[i] = (*grid)[i];
@@ -1425,6 +1431,59 @@ int nmm_write_vector(const char* path, const double* x, long long n) {
   size_t w = std::fwrite(x, 8, (size_t)n, f);
   std::fclose(f);
   return w == (size_t)n ? NMM_OK : fail(NMM_ERR_IO, "short write");
+}
+
+// Fortran list-directed output of a REAL(4) value as gfortran writes it
+// (nine significant digits, F form for 0.1 <= |x| < 1e9, else E form), which
+// is how the reference spells the frequencies in its output file names
+// (src/mod_para.f90:282-288).
+static std::string fortran_real4(double v) {
+  const double x = (double)(float)v;
+  const double ax = std::fabs(x);
+  char buf[64];
+  if (ax == 0.0) {
+    std::snprintf(buf, sizeof buf, "0.00000000");
+  } else if (ax >= 0.1 && ax < 1e9) {
+    const int e = (int)std::floor(std::log10(ax));
+    std::snprintf(buf, sizeof buf, "%.*f", std::max(0, 8 - e), x);
+  } else {
+    std::snprintf(buf, sizeof buf, "%.8E", x);
+  }
+  return buf;
+}
+
+int nmm_write_results(const nmm_model* m, const char* outputdir, const char* basename, int job, int nproc,
+                      double lowfreq, double upfreq, int nev, const double* X, long long ldx, char* prefix_out,
+                      int prefix_len) {
+  if (!m || !outputdir || !basename || nev < 0 || (nev > 0 && !X) || ldx < m->n || nproc < 1)
+    return fail(NMM_ERR_ARG, "bad argument");
+  const std::string p = std::to_string(m->porder), np = std::to_string(nproc);
+  const std::string dir = outputdir, base = dir + basename;
+  const std::string data = base + "_JOB" + std::to_string(job) + "_pod" + p + "_np" + np + "_" +
+                           fortran_real4(lowfreq) + "_" + fortran_real4(upfreq);
+  for (int i = 0; i < nev; ++i) {
+    const std::string f = data + "_" + std::to_string(i + 1) + ".dat";
+    const int rc = nmm_write_vector(f.c_str(), X + (size_t)i * ldx, m->n);
+    if (rc) return rc;
+  }
+  // node lists in DOF order: the input id (1-based) and the status of every
+  // node, int32 (src/mod_pevsl.f90:225-247)
+  auto write_i32 = [&](const std::string& f, const std::vector<int>& v) -> int {
+    FILE* fp = std::fopen(f.c_str(), "wb");
+    if (!fp) return fail(NMM_ERR_IO, "cannot open " + f);
+    const size_t w = std::fwrite(v.data(), 4, v.size(), fp);
+    std::fclose(fp);
+    return w == v.size() ? NMM_OK : fail(NMM_ERR_IO, "short write");
+  };
+  std::vector<int> vlist(m->nnode);
+  for (int i = 0; i < m->nnode; ++i) vlist[i] = (m->orig.empty() ? i : m->orig[i]) + 1;
+  int rc = write_i32(base + "_pod" + p + "_np" + np + "_vlist.dat", vlist);
+  if (rc) return rc;
+  if (m->fsexist && (rc = write_i32(base + "_pod" + p + "_np" + np + "_vstat.dat", m->vstat))) return rc;
+  if (prefix_out && prefix_len > 0) {
+    std::snprintf(prefix_out, (size_t)prefix_len, "%s", data.c_str());
+  }
+  return NMM_OK;
 }
 
 void nmm_destroy(nmm_model* m) { delete m; }

@@ -69,6 +69,8 @@ def lib() -> C.CDLL:
         L.nmm_element_matrices.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                            C.POINTER(C.c_int)]
         L.nmm_reference.argtypes = [vp] + [C.c_void_p] * 5
+        L.nmm_write_results.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double,
+                                        C.c_int, C.POINTER(C.c_double), C.c_longlong, C.c_char_p, C.c_int]
         L.nmm_set_material.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.nmm_write_vector.argtypes = [C.c_char_p, C.POINTER(C.c_double), C.c_longlong]
         L.nmm_last_error.restype = C.c_char_p
@@ -187,6 +189,20 @@ class Model:
         _check(lib().nmm_set_material(self._h, *[a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs]))
         if assemble:
             self.assemble()
+
+    def write_results(self, outputdir: str, basename: str, lowfreq: float, upfreq: float, X,
+                      job: int = 1, nproc: int = 1) -> str:
+        """Write eigenvectors (n x k, unscaled) and the node lists in the
+        reference's file layout; returns the eigenvector file prefix."""
+        X = np.asfortranarray(X, dtype=np.float64)
+        if X.ndim == 1:
+            X = X[:, None]
+        buf = C.create_string_buffer(4096)
+        d = outputdir if outputdir.endswith("/") or not outputdir else outputdir + "/"
+        _check(lib().nmm_write_results(self._h, d.encode(), basename.encode(), job, nproc, lowfreq, upfreq,
+                                       X.shape[1], X.ctypes.data_as(C.POINTER(C.c_double)), X.shape[0], buf,
+                                       len(buf)))
+        return buf.value.decode()
 
     def element_matrices(self, k: int):
         i = self.info()

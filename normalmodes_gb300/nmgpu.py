@@ -59,7 +59,8 @@ class NmResult(C.Structure):
                 ("t_bounds", C.c_double), ("t_filter_design", C.c_double), ("t_lanczos", C.c_double),
                 ("t_ritz", C.c_double), ("t_total", C.c_double),
                 ("n_amv", C.c_longlong), ("n_bsolve", C.c_longlong), ("n_spmv", C.c_longlong),
-                ("n_kernels", C.c_longlong), ("t_filter", C.c_double), ("t_orth", C.c_double)]
+                ("n_kernels", C.c_longlong), ("t_filter", C.c_double), ("t_orth", C.c_double),
+                ("t_eig", C.c_double)]
 
 
 class NmElemModel(C.Structure):
@@ -274,7 +275,8 @@ class Solver:
         return SolveResult(arr(r.lam), vec, arr(r.err_ref), arr(r.res2), tuple(r.xintv), r.pol_deg, r.pol_gam,
                            r.pol_bar, r.lanczos_steps, r.nritz_above_bar,
                            {"bounds": r.t_bounds, "filter_design": r.t_filter_design, "lanczos": r.t_lanczos,
-                            "ritz": r.t_ritz, "total": r.t_total, "filter": r.t_filter, "orth": r.t_orth},
+                            "ritz": r.t_ritz, "total": r.t_total, "filter": r.t_filter, "orth": r.t_orth,
+                            "eig": r.t_eig},
                            {"amv": r.n_amv, "bsolve": r.n_bsolve, "spmv": r.n_spmv, "kernels": r.n_kernels})
 
     def solve(self, lowfreq: float, upfreq: float, maxit: int = 0, tol: float = 0.0, ab_bounds=None,

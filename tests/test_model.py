@@ -163,3 +163,25 @@ def test_reference_format_roundtrip(tmp_path):
         a, b = m.csr(name), m2.csr(name)
         assert np.array_equal(a.col, b.col) and np.array_equal(a.rowptr, b.rowptr)
         assert np.max(np.abs(a.val - b.val)) <= 1e-14 * np.max(np.abs(a.val))
+
+
+def test_write_results_reference_layout(tmp_path):
+    """Eigenvector files, vlist and vstat in the reference's names and
+    formats (src/mod_pevsl.f90:188-247, src/mod_para.f90:269-288)."""
+    from normalmodes_gb300.model import Model
+    m = Model.ball(n_cells=8, porder=2)
+    info = m.info()
+    X = np.random.default_rng(2).standard_normal((info.n, 3))
+    prefix = m.write_results(str(tmp_path), "ball", 0.1, 2.0, X, job=1, nproc=1)
+    assert prefix.endswith("ball_JOB1_pod2_np1_0.100000001_2.00000000")
+    for i in range(3):
+        y = np.fromfile(f"{prefix}_{i + 1}.dat", dtype=np.float64)
+        assert np.array_equal(y, X[:, i])
+    vlist = np.fromfile(tmp_path / "ball_pod2_np1_vlist.dat", dtype=np.int32)
+    assert np.array_equal(np.sort(vlist), np.arange(1, info.nnode + 1))
+    # the input numbering puts the vertices first: their ids are 1..nvert
+    mesh = m.mesh()
+    vert_nodes = np.unique(mesh["tets"][:, [0, 2, 5, 9]])
+    assert vlist[vert_nodes].max() == info.nvert
+    vstat = np.fromfile(tmp_path / "ball_pod2_np1_vstat.dat", dtype=np.int32)
+    assert vstat.size == info.nnode and vstat.min() >= 0 and vstat.max() <= 5
