@@ -78,6 +78,9 @@ typedef struct {
   int use_graph;      /* capture the filter in a CUDA graph (default on)           */
   int block;          /* 0/1: single-vector ChebLanNr (the reference's algorithm);
                          32: block filtered Lanczos, 32 vectors per filter pass  */
+  int polish;         /* mixed block path: degree of the FP64-accurate refinement
+                         of the Ritz vectors (0: 80, <0: off; capped at
+                         2 sqrt(lmax / (b - a)) for narrow spectra)             */
 } nm_solve_opts;
 
 typedef struct {

@@ -32,7 +32,7 @@ module nmgpu_mod
     real(c_double) :: tol, thresh_int, thresh_ext
     integer(c_int) :: mlan_bounds
     real(c_double) :: ab_bounds(2)
-    integer(c_int) :: damping, want_vectors, unscale, use_graph, block
+    integer(c_int) :: damping, want_vectors, unscale, use_graph, block, polish
   end type nm_solve_opts
 
   type, bind(C) :: nm_result

@@ -26,6 +26,9 @@ def main(argv=None) -> None:
     ap.add_argument("--lateral", type=float, default=0.02)
     ap.add_argument("--interval", type=float, nargs=2, default=(0.1, 1.0))
     ap.add_argument("--fp64-block", type=int, default=32)
+    ap.add_argument("--polish", type=int, default=0, help="mixed path refinement degree (0: default, <0: off)")
+    ap.add_argument("--fp64-lam", default=None, help="eigenvalues of an earlier FP64 solve (.npy) instead of solving")
+    ap.add_argument("--save-fp64-lam", default=None, help="write the FP64 eigenvalues to this .npy file")
     a = ap.parse_args(argv)
     from normalmodes_gb300.model import Model
     from normalmodes_gb300.nmgpu import NM_PREC_FP64, NM_PREC_MIXED, Solver
@@ -34,12 +37,13 @@ def main(argv=None) -> None:
         kw.update(lateral_pert=a.lateral, lateral_lmax=8)
     mats = Model.ball(**kw).operators()
     lo, hi = a.interval
-    out = {"cells": a.cells, "porder": a.porder, "lateral": a.lateral, "interval_mhz": [lo, hi]}
+    out = {"cells": a.cells, "porder": a.porder, "lateral": a.lateral, "interval_mhz": [lo, hi], "polish": a.polish}
     res = {}
-    for name, prec, block in (("mixed", NM_PREC_MIXED, 32), ("fp64", NM_PREC_FP64, a.fp64_block)):
+    runs = [("mixed", NM_PREC_MIXED, 32)] + ([] if a.fp64_lam else [("fp64", NM_PREC_FP64, a.fp64_block)])
+    for name, prec, block in runs:
         with Solver(mats, a.porder, precision=prec) as sv:
             t = time.perf_counter()
-            r = sv.solve(lo, hi, block=block, want_vectors=False)
+            r = sv.solve(lo, hi, block=block, want_vectors=False, polish=a.polish if name == "mixed" else 0)
             dt = time.perf_counter() - t
         res[name] = r
         out[name] = {"nev": len(r.lam), "seconds": round(dt, 3), "block": block, "lanczos_vectors": r.lanczos_steps,
@@ -48,14 +52,18 @@ def main(argv=None) -> None:
                      "err_ref_median": float(np.median(r.err_ref)) if len(r.lam) else None,
                      "res2_max": float(r.res2.max()) if len(r.lam) else None,
                      "res2_median": float(np.median(r.res2)) if len(r.lam) else None}
-    m, f = res["mixed"].lam, res["fp64"].lam
+    m = res["mixed"].lam
+    f = np.load(a.fp64_lam) if a.fp64_lam else res["fp64"].lam
+    if a.save_fp64_lam and "fp64" in res:
+        np.save(a.save_fp64_lam, f)
     out["same_count"] = len(m) == len(f)
     if len(m) == len(f) and len(f):
         rel = np.abs(m - f) / np.abs(f)
         out["eig_rel_diff_max"] = float(rel.max())
         out["eig_rel_diff_median"] = float(np.median(rel))
         out["eig_rel_diff"] = [float(x) for x in rel]
-    out["speedup_mixed_over_fp64"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
+    if "fp64" in out:
+        out["speedup_mixed_over_fp64"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
     print(json.dumps(out))
 
 

@@ -291,17 +291,14 @@ __device__ __forceinline__ XT ld(const XT* p) {
 // between them and can be in flight together.  CTAs take consecutive rows;
 // rows are numbered along a space-filling curve, so the rows in flight at
 // any time form a compact piece of the mesh whose neighbour rows stay in L2.
-template <typename VT, typename XT, int NC, int MODE, int UNR = 4>
+template <typename VT, typename XT, int NC, int MODE>
 __global__ void __launch_bounds__(kT)
     k_mass_cheb(int ng, const int* __restrict__ rp, const int* __restrict__ ci, const VT* __restrict__ mv,
                 const XT* __restrict__ b, const XT* __restrict__ xcur, const XT* xprev, XT* xout, XT a, XT c,
-                XT inv_theta, int rpw) {
+                XT inv_theta) {
+  constexpr int UNR = 4;  // gathers in flight per warp
   const int lane = threadIdx.x & (kBlk - 1);
-  const int wpc = blockDim.x >> 5;  // warps per CTA
-  // the CTA owns wpc * rpw consecutive rows; its warps take them wpc at a
-  // time, so the rows in flight stay adjacent and the window slides
-  for (int r = 0; r < rpw; ++r) {
-  const int g = (blockIdx.x * rpw + r) * wpc + (threadIdx.x >> 5);
+  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (g >= ng) return;
   const XT* src = MODE == 0 ? b : xcur;
   XT bo[NC], xc[NC], xp[NC];
@@ -352,7 +349,6 @@ __global__ void __launch_bounds__(kT)
     const XT tt = MODE == 0 ? t[p] * inv_theta : t[p];
     // x_{j+1} = x_j + a (x_j - x_{j-1}) + c (b - M x_j)
     xout[i0 + p * kBlk] = fm<XT>(c, bo[p] - tt, fm<XT>(a, xc[p] - xp[p], xc[p]));
-  }
   }
 }
 
@@ -733,7 +729,8 @@ __global__ void __launch_bounds__(kT)
     k_amv3(int ng, const int* __restrict__ arp, const int* __restrict__ aci, const VT* __restrict__ av,
            const int* __restrict__ erp, const int* __restrict__ eci, const VT* __restrict__ ev,
            const XT* __restrict__ v, const XT* __restrict__ y, XT* __restrict__ out, const XT* __restrict__ vk,
-           const XT* __restrict__ vkm1, XT* __restrict__ yacc, XT s, XT cc, XT pm, XT mu) {
+           const XT* __restrict__ vkm1, XT* __restrict__ yacc, XT s, XT cc, XT pm, XT mu,
+           const XT* __restrict__ fz, XT fco) {
   const int lane = threadIdx.x & (kBlk - 1);
   const int g = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5);
   if (g >= ng) return;
@@ -798,7 +795,8 @@ __global__ void __launch_bounds__(kT)
     if (MODE == 0) {
       out[idx] = ww[p];
     } else {
-      const XT t = fm<XT>(s, fm<XT>(-cc, vk[idx], ww[p]), -pm * vkm1[idx]);
+      XT t = fm<XT>(s, fm<XT>(-cc, vk[idx], ww[p]), -pm * vkm1[idx]);
+      if (fz) t = fm<XT>(fco, fz[idx], t);
       out[idx] = t;
       yacc[idx] = fm<XT>(mu, t, yacc[idx]);
     }
@@ -856,6 +854,22 @@ __global__ void k_from_colmajor(const double* __restrict__ src, size_t ld, int n
   }
 }
 
+// Range form of the filter: vk = a1 z, vkm1 = 0, y = mu1 vk.
+template <typename XT>
+__global__ void k_init_range_blk(XT* vk, XT* vkm1, XT* y, const XT* z, XT a1, XT mu1, size_t len) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= len) return;
+  const XT v = a1 * z[i];
+  vk[i] = v;
+  vkm1[i] = (XT)0;
+  y[i] = mu1 * v;
+}
+// dst (row-major FP64 block) = (double) src (row-major FP32 block)
+__global__ void k_f2d_flat(const float* __restrict__ src, double* __restrict__ dst, size_t len) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < len) dst[i] = (double)src[i];
+}
+
 template <typename XT>
 __global__ void k_init_filter_blk(XT* vk, XT* vkm1, XT* y, const XT* v, XT mu0, size_t len) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -892,26 +906,6 @@ bool gather_vec(int nc) {
   return v < 0 ? nc == 1 : v != 0;
 }
 
-// Rows each warp of k_mass_cheb takes in turn (NM_GATHER_RPW, 1..16).
-int gather_rpw() {
-  static int v = 0;
-  if (!v) {
-    v = 1;
-    if (const char* e = std::getenv("NM_GATHER_RPW")) v = std::min(16, std::max(1, std::atoi(e)));
-  }
-  return v;
-}
-
-// Gathers in flight per warp in k_mass_cheb (4 or 8; NM_GATHER_UNROLL).
-int gather_unroll() {
-  static int v = 0;
-  if (!v) {
-    v = 4;
-    if (const char* e = std::getenv("NM_GATHER_UNROLL")) v = std::atoi(e) == 8 ? 8 : 4;
-  }
-  return v;
-}
-
 template <typename VT, typename XT, int NC>
 void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s) {
   const int ng = M.nrows;
@@ -920,9 +914,7 @@ void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT*
   XT* buf[2] = {work, work + len};  // x_j lives in buf[j & 1]
   const XT it = (XT)ch.inv_theta;
   const int thr = gather_threads(), rows = thr / 32;
-  const int rpw = NC == 3 ? gather_rpw() : 1;  // rows per warp of k_mass_cheb
   const int grid = (ng + rows - 1) / rows;
-  const int grid_m = (ng + rows * rpw - 1) / (rows * rpw);
   for (int j = 1; j <= ch.deg; ++j) {
     const XT a = (XT)ch.a[j - 1], c = (XT)ch.c[j - 1];
     XT* out = j == ch.deg ? x : buf[(j + 1) & 1];
@@ -930,20 +922,16 @@ void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT*
     const XT* prev = buf[(j + 1) & 1];
 #define NM_MV(MODE) \
   k_gcheb<VT, XT, NC, MODE><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it)
-#define NM_MC(MODE, U) \
-  k_mass_cheb<VT, XT, NC, MODE, U><<<grid_m, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it, rpw)
+#define NM_MC(MODE) \
+  k_mass_cheb<VT, XT, NC, MODE><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it)
     if (gather_vec(NC)) {
       if (j == 1) NM_MV(0);
       else if (j == 2) NM_MV(1);
       else NM_MV(2);
-    } else if (gather_unroll() == 8) {
-      if (j == 1) NM_MC(0, 8);
-      else if (j == 2) NM_MC(1, 8);
-      else NM_MC(2, 8);
     } else {
-      if (j == 1) NM_MC(0, 4);
-      else if (j == 2) NM_MC(1, 4);
-      else NM_MC(2, 4);
+      if (j == 1) NM_MC(0);
+      else if (j == 2) NM_MC(1);
+      else NM_MC(2);
     }
 #undef NM_MC
 #undef NM_MV
@@ -1085,13 +1073,14 @@ template <typename VT, typename XT>
 void blk_amv(const GCsr<VT>& A, const GCsr<VT>* E, const XT* v, const XT* y, XT* out, const XT* vk, const XT* vkm1,
              XT* yacc, const FiltEpi& ep, cudaStream_t s) {
   const int ng = A.nrows;
-  const XT S = (XT)ep.s, CC = (XT)ep.cc, PM = (XT)ep.pm, MU = (XT)ep.mu;
+  const XT S = (XT)ep.s, CC = (XT)ep.cc, PM = (XT)ep.pm, MU = (XT)ep.mu, FC = (XT)ep.fco;
+  const XT* FZ = (const XT*)ep.fz;
   const int* erp = E ? E->rp : nullptr;
   const int* eci = E ? E->ci : nullptr;
   const VT* ev = E ? E->v : nullptr;
 #define NM_AMV(HE, MO)                                                                                            \
   k_amv3<VT, XT, HE, MO><<<nrb(ng), kT, 0, s>>>(ng, A.rp, A.ci, A.v, erp, eci, ev, v, y, out, vk, vkm1, yacc, S, \
-                                                CC, PM, MU)
+                                                CC, PM, MU, FZ, FC)
   if (E) {
     if (ep.mode == 0) NM_AMV(true, 0);
     else NM_AMV(true, 1);
@@ -1132,6 +1121,52 @@ __global__ void k_sub_f32(double* __restrict__ W, size_t ldw, const float* __res
 }
 }  // namespace
 
+namespace {
+// R = (float)(AU - theta_col BU) on row-major 32-column blocks
+__global__ void k_resid_f32(const double* __restrict__ AU, const double* __restrict__ BU,
+                            const double* __restrict__ theta, float* __restrict__ R, float scale, size_t len) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= len) return;
+  R[i] = (float)(AU[i] - theta[i & (kBlk - 1)] * BU[i]) * scale;
+}
+// v += f_col R
+__global__ void k_force(float* __restrict__ v, const float* __restrict__ R, const float* __restrict__ f, size_t len) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= len) return;
+  v[i] = fmaf(f[i & (kBlk - 1)], R[i], v[i]);
+}
+// U(:, col) += sc_col G(:, col): G row-major 32-column block, U column-major
+__global__ void k_add_colmajor(const float* __restrict__ G, const double* __restrict__ sc, int n,
+                               double* __restrict__ U, size_t ld) {
+  __shared__ float tile[kBlk][kBlk + 1];
+  const int i0 = blockIdx.x * kBlk;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int r = ty; r < kBlk; r += 8) {
+    const int i = i0 + r;
+    tile[r][tx] = i < n ? G[(size_t)i * kBlk + tx] : 0.0f;
+  }
+  __syncthreads();
+  for (int c = ty; c < kBlk; c += 8) {
+    const int i = i0 + tx;
+    if (i < n) U[(size_t)c * ld + i] += sc[c] * (double)tile[tx][c];
+  }
+}
+}  // namespace
+
+void blk_resid_f32(const double* AU, const double* BU, const double* theta, float* R, float scale, size_t len,
+                   cudaStream_t s) {
+  k_resid_f32<<<(int)((len + 255) / 256), 256, 0, s>>>(AU, BU, theta, R, scale, len);
+  nmg::add_launches(1);
+}
+void blk_force(float* v, const float* R, const float* f, size_t len, cudaStream_t s) {
+  k_force<<<(int)((len + 255) / 256), 256, 0, s>>>(v, R, f, len);
+  nmg::add_launches(1);
+}
+void blk_add_colmajor(const float* G, const double* sc, int n, double* U, size_t ld, cudaStream_t s) {
+  k_add_colmajor<<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(G, sc, n, U, ld);
+  nmg::add_launches(1);
+}
+
 void blk_d2f(const double* src, size_t lds, float* dst, size_t ldd, int n, int cols, cudaStream_t s) {
   const long long tot = (long long)n * cols;
   k_d2f<<<(int)((tot + 255) / 256), 256, 0, s>>>(src, lds, dst, ldd, n, cols);
@@ -1160,6 +1195,17 @@ void blk_from_colmajor(const double* src, size_t ld, int n, XT* blk, cudaStream_
 }
 template void blk_from_colmajor<float>(const double*, size_t, int, float*, cudaStream_t);
 template void blk_from_colmajor<double>(const double*, size_t, int, double*, cudaStream_t);
+
+template <typename XT>
+void blk_init_range(XT* vk, XT* vkm1, XT* y, const XT* z, double a1, double mu1, size_t len, cudaStream_t s) {
+  k_init_range_blk<XT><<<(int)((len + 255) / 256), 256, 0, s>>>(vk, vkm1, y, z, (XT)a1, (XT)mu1, len);
+  nmg::add_launches(1);
+}
+template void blk_init_range<float>(float*, float*, float*, const float*, double, double, size_t, cudaStream_t);
+void blk_f2d_flat(const float* src, double* dst, size_t len, cudaStream_t s) {
+  k_f2d_flat<<<(int)((len + 255) / 256), 256, 0, s>>>(src, dst, len);
+  nmg::add_launches(1);
+}
 
 template <typename XT>
 void blk_init_filter(XT* vk, XT* vkm1, XT* y, const XT* v, double mu0, size_t len, cudaStream_t s) {

@@ -118,6 +118,10 @@ template <typename XT>
 void blk_to_colmajor(const XT* blk, int n, double* out, size_t ld, cudaStream_t s);  // out(:, c) = blk(:, c)
 template <typename XT>
 void blk_init_filter(XT* vk, XT* vkm1, XT* y, const XT* v, double mu0, size_t len, cudaStream_t s);
+// Range form of the filter: vk = a1 z, vkm1 = 0, y = mu1 vk.
+template <typename XT>
+void blk_init_range(XT* vk, XT* vkm1, XT* y, const XT* z, double a1, double mu1, size_t len, cudaStream_t s);
+void blk_f2d_flat(const float* src, double* dst, size_t len, cudaStream_t s);
 template <typename XT>
 void blk_from_colmajor(const double* src, size_t ld, int n, XT* blk, cudaStream_t s);  // blk = src(:, 0:S)^T
 int blk_coop_blocks();
@@ -135,6 +139,12 @@ struct Basis32 {
 void blk_d2f(const double* src, size_t lds, float* dst, size_t ldd, int n, int cols, cudaStream_t s);
 void blk_sub_f32(double* W, size_t ldw, const float* T, size_t ldt, int n, int cols, cudaStream_t s);
 void blk_f2d(const float* src, size_t lds, double* dst, size_t ldd, int n, int cols, cudaStream_t s);
+// Polish helpers (row-major 32-column blocks): R = scale (AU - theta_col BU)
+// in FP32; v += f_col R; U(:, col) += sc_col G(:, col) into column-major U.
+void blk_resid_f32(const double* AU, const double* BU, const double* theta, float* R, float scale, size_t len,
+                   cudaStream_t s);
+void blk_force(float* v, const float* R, const float* f, size_t len, cudaStream_t s);
+void blk_add_colmajor(const float* G, const double* sc, int n, double* U, size_t ld, cudaStream_t s);
 
 // Grouped operators and buffers of the batched path.
 struct BlockState {
@@ -165,6 +175,13 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
 // FP64 Rayleigh-Ritz on the columns of U (n x nc): U <- U Q with
 // (U^T A U) Q = (U^T B U) Q Theta.  Resolves the mixing of close Ritz pairs
 // left by an FP32 filter.
-int rayleigh_ritz64(nm_ctx* c, double** U, int nc);
+int rayleigh_ritz64(nm_ctx* c, double** U, int nc, std::vector<double>* theta = nullptr);
+// Mixed path: refine the Ritz vectors U (n x nc, B-normalised, Ritz values
+// theta) towards FP64 accuracy: U <- U + B~^-1 D / tau, the part of
+// q(A B~^-1) B U that differs from q(theta) B U, with q the degree-deg
+// Chebyshev polynomial of [cfrac lmax, lmax].  D follows the three-term
+// recurrence driven by the FP64 residual A U - theta B U and runs in FP32
+// (it is small, so FP32 rounding stays at FP64 level relative to U).
+int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, int deg, double cfrac);
 
 }  // namespace nmg

@@ -78,9 +78,13 @@ int block_build(nm_ctx* c, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, c
         ((rc = upload_g(c, hE, st->E32)) || (rc = upload_g(c, hET, st->ET32)) || (rc = upload_g(c, hAp, st->Ap32))))
       return rc;
   }
-  if (c->precision == NM_PREC_MIXED) {
-    // staged FP32 Chebyshev solves: tiles of consecutive rows whose distinct
-    // neighbour rows fit in shared memory (R halves until they fit)
+  const char* mk = std::getenv("NM_MASS_KERNEL");
+  const char* ak = std::getenv("NM_AP_KERNEL");
+  if (c->precision == NM_PREC_MIXED && ((mk && std::atoi(mk) == 1) || (ak && std::atoi(ak) == 1))) {
+    // staged FP32 Chebyshev solves (selected with NM_MASS_KERNEL / NM_AP_KERNEL
+    // = 1; measured slower than the gather kernels on GB300): tiles of
+    // consecutive rows whose distinct neighbour rows fit in shared memory
+    // (R halves until they fit)
     const size_t smem_max = 110 * 1024;
     int rM = 32, rAp = 32;
     if (const char* e = std::getenv("NM_TILE_ROWS_M")) rM = std::max(4, std::atoi(e));
@@ -247,6 +251,72 @@ void block_filter(nm_ctx* c, const Pol& pol, const GCsr<VT>& M, const GCsr<VT>& 
     vk = vkp1;
     vkp1 = t;
   }
+}
+
+// Mixed path, range form of the filter.  With p(x) = p(0) + x r(x) the
+// filtered block is W = p(A B~^-1) Z = p(0) Z + A B~^-1 Y, Y = r(A B~^-1) Z.
+// Y = sum_k mu_k E_k follows the Chebyshev recurrence of the filter with a
+// forcing term, E_1 = alpha z, E_{k+1} = 2 L E_k - E_{k-1} + 2 alpha tau_k z
+// (L = alpha (A B~^-1 - cc), alpha = 1/dd, tau_k = T_k(-cc/dd)), in FP32;
+// the last product A B~^-1 Y runs with the FP64 operator.  So W has exactly
+// p(0) times the null-space content of Z: the FP32 rounding of the
+// recurrence cannot leak into the zero-frequency fluid modes (whose
+// components would lower every Rayleigh quotient), and p(0) Z is added in
+// FP64 by the caller.  Leaves A B~^-1 Y in sout64 (row-major FP64).
+void block_filter_range(nm_ctx* c, const Pol& pol, FiltBufs<float> f, double* sin64, double* sout64,
+                        double* x064, double* y064, double* apw64) {
+  BlockState* st = bs(c);
+  cudaStream_t s = c->stream;
+  const size_t L = (size_t)kBlk * c->n;
+  const double a1 = 1.0 / pol.dd, l0 = -pol.cc / pol.dd;
+  blk_init_range<float>(f.vk, f.vkm1, f.yout, f.zin, a1, pol.deg >= 1 ? pol.mu[1] : 0.0, L, s);
+  double tkm1 = 1.0, tk = l0;  // tau_{k-1}, tau_k
+  float *vk = f.vk, *vkm1 = f.vkm1, *vkp1 = f.vkp1;
+  for (int k = 1; k < pol.deg; ++k) {
+    blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
+    if (c->fs) {
+      blk_et<float, float>(st->ET32, f.w2, f.x0, s);
+      blk_ap_solve<float, float>(c, st->Ap32, f.x0, f.y0, f.apwork);
+    }
+    FiltEpi ep;
+    ep.mode = 1;
+    ep.s = 2.0 / pol.dd;
+    ep.cc = pol.cc;
+    ep.pm = 1.0;
+    ep.mu = pol.mu[k + 1];
+    ep.fz = f.zin;
+    ep.fco = 2.0 * a1 * tk;
+    blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s);
+    float* t = vkm1;
+    vkm1 = vk;
+    vk = vkp1;
+    vkp1 = t;
+    const double tn = 2.0 * l0 * tk - tkm1;
+    tkm1 = tk;
+    tk = tn;
+  }
+  // A B~^-1 Y: B~^-1 in FP32 (its error stays inside the argument of A), A in FP64
+  blk_mass_solve<float, float>(c, st->M32, f.yout, f.w2, f.bwork);
+  blk_f2d_flat(f.w2, sin64, L, s);
+  if (c->fs) {
+    blk_et<double, double>(st->ET64, sin64, x064, s);
+    blk_ap_solve<double, double>(c, st->Ap64, x064, y064, apw64);
+  }
+  FiltEpi ep0;
+  blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin64, y064, sout64, nullptr, nullptr, nullptr, ep0, s);
+}
+
+// p(0) of the filter polynomial: sum_k mu_k T_k(-cc/dd).
+double filter_at_zero(const Pol& pol) {
+  const double l0 = -pol.cc / pol.dd;
+  double tkm1 = 1.0, tk = l0, p0 = pol.mu.empty() ? 0.0 : pol.mu[0];
+  for (int k = 1; k <= pol.deg; ++k) {
+    p0 += pol.mu[k] * tk;
+    const double tn = 2.0 * l0 * tk - tkm1;
+    tkm1 = tk;
+    tk = tn;
+  }
+  return p0;
 }
 
 }  // namespace
@@ -447,6 +517,13 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   double* sin_ = carve(p64, L);     // row-major block for the FP64 B solve
   double* sout = carve(p64, L);
   double* swork = carve(p64, 4 * L);
+  const size_t Pn = (size_t)S * (np ? np : 1);
+  double* x064 = carve(p64, Pn);    // pressure blocks of the FP64 A-op
+  double* y064 = carve(p64, Pn);
+  double* apw64 = carve(p64, 4 * Pn);
+  // mixed path: range form of the filter (FP64 last A-op, p(0) Z added in FP64)
+  const bool range_form = mixed && std::getenv("NM_FILTER_PLAIN") == nullptr;
+  const double p0 = filter_at_zero(pol);
   const size_t ldw = n;
   // ---- small device matrices: S x S scratch and H (K x S), T for cuSOLVER
   const int max_blocks = std::max(1, std::min(maxit, kMaxCols - S) / S);
@@ -538,7 +615,9 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   cudaGraphExec_t gexec = nullptr;
   long long graph_nodes = 0;
   auto run_filter = [&]() {
-    if (mixed)
+    if (range_form)
+      block_filter_range(c, pol, f32b, sin_, sout, x064, y064, apw64);
+    else if (mixed)
       block_filter<float, float>(c, pol, st->M32, st->A32, st->Ap32, st->E32, st->ET32, f32b);
     else
       block_filter<double, double>(c, pol, st->M64, st->A64, st->Ap64, st->E64, st->ET64, f64b);
@@ -656,8 +735,16 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
     c->n_bsolve += (long long)pol.deg * S;
     c->n_spmv += (long long)pol.deg * (mixed ? mass_cheb<float>(c).deg + (c->fs ? 2 + ap_cheb<float>(c).deg : 1)
                                              : c->chebB.deg + (c->fs ? 2 + c->chebAp.deg : 1));
-    if (mixed) blk_to_colmajor<float>(f32b.yout, n, Wc, ldw, s);
-    else blk_to_colmajor<double>(f64b.yout, n, Wc, ldw, s);
+    if (range_form) {
+      // W = A B~^-1 Y + p(0) Z_j, the Z_j term from the FP64 basis
+      blk_to_colmajor<double>(sout, n, Wc, ldw, s);
+      CB(c, cublasDgeam(hb, CUBLAS_OP_N, CUBLAS_OP_N, n, S, &one, Wc, (int)ldw, &p0, Z.col(j * S), (int)Z.ld, Wc,
+                        (int)ldw));
+    } else if (mixed) {
+      blk_to_colmajor<float>(f32b.yout, n, Wc, ldw, s);
+    } else {
+      blk_to_colmajor<double>(f64b.yout, n, Wc, ldw, s);
+    }
     NM_CUDA(c, cudaEventRecord(ev[1], s));
     // W -= Z_{j-1} R_j^T
     if (j > 0) {
@@ -806,7 +893,7 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   return NM_OK;
 }
 
-int rayleigh_ritz64(nm_ctx* c, double** Uio, int nc) {
+int rayleigh_ritz64(nm_ctx* c, double** Uio, int nc, std::vector<double>* theta) {
   BlockState* st = bs(c);
   if (!st || !st->ok || !st->cublas || nc <= 0) return NM_OK;
   const int n = c->n, np = c->np, S = kBlk;
@@ -876,7 +963,118 @@ int rayleigh_ritz64(nm_ctx* c, double** Uio, int nc) {
   }
   // U <- U Q  (Q in GA, B-orthonormal columns)
   CB(c, cublasDgemm(st->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, nc, nc, &one, Up, n, GA, nc, &zero, U, n));
+  if (theta) {
+    theta->resize(nc);
+    NM_CUDA(c, cudaMemcpyAsync(theta->data(), W, sizeof(double) * nc, cudaMemcpyDeviceToHost, s));
+  }
   NM_CUDA(c, cudaStreamSynchronize(s));
+  release();
+  return NM_OK;
+}
+
+int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, int deg, double cfrac) {
+  BlockState* st = bs(c);
+  if (!st || !st->ok || nc <= 0 || deg <= 0 || c->precision != NM_PREC_MIXED) return NM_OK;
+  if ((int)theta.size() < nc || !(lmax > 0.0) || !(cfrac > 0.0 && cfrac < 1.0))
+    return set_err(c, NM_ERR_ARG, "polish: bad arguments");
+  int rc;
+  if ((rc = block_buffers(c))) return rc;
+  const int n = c->n, np = c->np, S = kBlk;
+  const int ncp = (nc + S - 1) / S * S;
+  cudaStream_t s = c->stream;
+  const size_t L = (size_t)S * n, P = (size_t)S * (np ? np : 1);
+  // FP64 scratch: row-major U block, A U, B U, pressure work
+  double* p64 = st->f64 + 2 * L;
+  double* sin_ = carve(p64, L);
+  double* sAU = carve(p64, L);
+  double* sBU = carve(p64, 4 * L);  // first L of the B-solve work area
+  double* x0 = carve(p64, P);
+  double* y0 = carve(p64, P);
+  double* apw = carve(p64, 4 * P);
+  FiltBufs<float> f = filt_carve<float>(st->f32, n, np);
+  // polynomial q = T_deg(l(x)), l(x) = alpha x - beta maps [c0, lmax] to [-1, 1]
+  const double c0 = cfrac * lmax, alpha = 2.0 / (lmax - c0), beta = (lmax + c0) / (lmax - c0);
+  double *Up = nullptr, *dth = nullptr, *dsc = nullptr;
+  float* dfor = nullptr;
+  auto release = [&]() {
+    cudaStreamSynchronize(s);
+    cudaFree(Up);
+    cudaFree(dth);
+    cudaFree(dsc);
+    cudaFree(dfor);
+  };
+  const size_t nb = sizeof(double) * (size_t)n * ncp;
+  if (cudaMalloc(&Up, nb) != cudaSuccess || cudaMalloc(&dth, sizeof(double) * S) != cudaSuccess ||
+      cudaMalloc(&dsc, sizeof(double) * S) != cudaSuccess ||
+      cudaMalloc(&dfor, sizeof(float) * (size_t)S * std::max(deg, 1)) != cudaSuccess) {
+    release();
+    return set_err(c, NM_ERR_OOM, "polish workspace");
+  }
+  NM_CUDA(c, cudaMemsetAsync(Up, 0, nb, s));
+  NM_CUDA(c, cudaMemcpyAsync(Up, U, sizeof(double) * (size_t)n * nc, cudaMemcpyDeviceToDevice, s));
+  FiltEpi ep0;  // plain product
+  FiltEpi ep;   // D_{j+1} = 2 alpha A B~^-1 D_j - 2 beta D_j - D_{j-1}
+  ep.mode = 1;
+  ep.s = 2.0 * alpha;
+  ep.cc = beta / alpha;
+  ep.pm = 1.0;
+  ep.mu = 0.0;
+  std::vector<double> th(S), sc(S);
+  std::vector<float> forc((size_t)S * deg);
+  for (int j0 = 0; j0 < ncp; j0 += S) {
+    // per-column scalars: tau_j = T_j(l(theta)), forcing 2 alpha tau_j
+    for (int col = 0; col < S; ++col) {
+      const double t = j0 + col < nc ? theta[j0 + col] : 0.0;
+      th[col] = t;
+      const double l = alpha * t - beta;
+      // a Ritz value inside (or at the edge of) the damped band would divide
+      // by a small T_deg(l): such a column is left as it is
+      const bool skip = !(l < -1.0 - 1e-6);
+      double tm1 = 1.0, tj = l;
+      for (int j = 1; j < deg; ++j) {
+        forc[(size_t)j * S + col] = skip ? 0.0f : (float)(2.0 * alpha * tj);
+        const double tn = 2.0 * l * tj - tm1;
+        tm1 = tj;
+        tj = tn;
+      }
+      sc[col] = skip ? 0.0 : 1.0 / tj;  // 1 / tau_deg
+    }
+    NM_CUDA(c, cudaMemcpyAsync(dth, th.data(), sizeof(double) * S, cudaMemcpyHostToDevice, s));
+    NM_CUDA(c, cudaMemcpyAsync(dsc, sc.data(), sizeof(double) * S, cudaMemcpyHostToDevice, s));
+    NM_CUDA(c, cudaMemcpyAsync(dfor, forc.data(), sizeof(float) * (size_t)S * deg, cudaMemcpyHostToDevice, s));
+    // FP64 residual R = A U - theta B U (reference operators and degrees)
+    blk_from_colmajor<double>(Up + (size_t)j0 * n, n, n, sin_, s);
+    if (c->fs) {
+      blk_et<double, double>(st->ET64, sin_, x0, s);
+      blk_ap_solve<double, double>(c, st->Ap64, x0, y0, apw);
+    }
+    blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sAU, nullptr, nullptr, nullptr, ep0, s);
+    blk_mass_spmv<double>(st->M64, sin_, sBU, s);
+    // FP32: D_0 = 0, D_1 = alpha R;  R kept in zin
+    blk_resid_f32(sAU, sBU, dth, f.zin, 1.0f, L, s);
+    blk_resid_f32(sAU, sBU, dth, f.vk, (float)alpha, L, s);
+    NM_CUDA(c, cudaMemsetAsync(f.vkm1, 0, sizeof(float) * L, s));
+    float *vk = f.vk, *vkm1 = f.vkm1, *vkp1 = f.vkp1;
+    for (int j = 1; j < deg; ++j) {
+      blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
+      if (c->fs) {
+        blk_et<float, float>(st->ET32, f.w2, f.x0, s);
+        blk_ap_solve<float, float>(c, st->Ap32, f.x0, f.y0, f.apwork);
+      }
+      blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s);
+      blk_force(vkp1, f.zin, dfor + (size_t)j * S, L, s);
+      float* t = vkm1;
+      vkm1 = vk;
+      vk = vkp1;
+      vkp1 = t;
+    }
+    // U += B~^-1 D_deg / tau_deg
+    blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
+    blk_add_colmajor(f.w2, dsc, n, Up + (size_t)j0 * n, n, s);
+  }
+  c->n_amv += (long long)ncp * deg;
+  NM_CUDA(c, cudaMemcpyAsync(U, Up, sizeof(double) * (size_t)n * nc, cudaMemcpyDeviceToDevice, s));
+  NM_CUDA(c, cudaGetLastError());
   release();
   return NM_OK;
 }

@@ -183,6 +183,8 @@ int upload_cheb(nm_ctx* c, ChebSetup& ch);
 struct FiltEpi {
   int mode = 0;        // 0: out = w; 1: filter recurrence
   double s = 0, cc = 0, pm = 0, mu = 0;
+  const void* fz = nullptr;  // block path, mode 1: forcing block (same precision as the vectors) or null
+  double fco = 0;            // out += fco * fz before the accumulation
 };
 template <typename VT, typename XT>
 void amv_fused(const Sell<VT>& A, const Sell<VT>* E, const XT* v, const XT* y, XT* out, const XT* vk,

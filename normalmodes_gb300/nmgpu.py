@@ -48,7 +48,8 @@ class NmOpts(C.Structure):
 class NmSolveOpts(C.Structure):
     _fields_ = [("maxit", C.c_int), ("tol", C.c_double), ("thresh_int", C.c_double), ("thresh_ext", C.c_double),
                 ("mlan_bounds", C.c_int), ("ab_bounds", C.c_double * 2), ("damping", C.c_int),
-                ("want_vectors", C.c_int), ("unscale", C.c_int), ("use_graph", C.c_int), ("block", C.c_int)]
+                ("want_vectors", C.c_int), ("unscale", C.c_int), ("use_graph", C.c_int), ("block", C.c_int),
+                ("polish", C.c_int)]
 
 
 class NmResult(C.Structure):
@@ -250,7 +251,7 @@ class Solver:
 
     @staticmethod
     def _solve_opts(maxit=0, tol=0.0, ab_bounds=None, want_vectors=True, unscale=False, use_graph=True, damping=1,
-                    mlan_bounds=0, block=0) -> "NmSolveOpts":
+                    mlan_bounds=0, block=0, polish=0) -> "NmSolveOpts":
         o = NmSolveOpts()
         lib().nm_default_solve_opts(C.byref(o))
         o.maxit = maxit
@@ -261,6 +262,7 @@ class Solver:
         o.damping = damping
         o.mlan_bounds = mlan_bounds
         o.block = block
+        o.polish = polish
         if ab_bounds is not None:
             o.ab_bounds[0], o.ab_bounds[1] = ab_bounds
         return o
@@ -281,9 +283,10 @@ class Solver:
 
     def solve(self, lowfreq: float, upfreq: float, maxit: int = 0, tol: float = 0.0, ab_bounds=None,
               want_vectors: bool = True, unscale: bool = False, use_graph: bool = True, damping: int = 1,
-              mlan_bounds: int = 0, allow_noconv: bool = False, block: int = 0) -> SolveResult:
+              mlan_bounds: int = 0, allow_noconv: bool = False, block: int = 0, polish: int = 0) -> SolveResult:
         L = lib()
-        o = self._solve_opts(maxit, tol, ab_bounds, want_vectors, unscale, use_graph, damping, mlan_bounds, block)
+        o = self._solve_opts(maxit, tol, ab_bounds, want_vectors, unscale, use_graph, damping, mlan_bounds, block,
+                             polish)
         r = NmResult()
         rc = L.nm_solve(self._h, lowfreq, upfreq, C.byref(o), C.byref(r))
         try:

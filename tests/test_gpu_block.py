@@ -42,4 +42,30 @@ def test_block_mixed_precision(small_models, name):
     assert len(res.lam) == len(g["lam"])
     rel = np.abs(res.lam - g["lam"]) / g["lam"]
     print(f"{name}: mixed eigenvalue rel err max {rel.max():.2e}, err_ref max {res.err_ref.max():.2e}")
-    assert rel.max() < 1e-9  # FP32 noise squared at the lowest modes; see the residual refinement
+    assert rel.max() < 1e-10
+
+
+@pytest.mark.parametrize("name", ["fs_p1", "fs_p2"])
+def test_mixed_polish_reaches_fp64_eigenvalues(small_models, name):
+    """Mixed path with the range-form filter (no FP32 rounding in the
+    zero-frequency fluid modes) and the FP64-accurate refinement of the Ritz
+    vectors (degree 80 by default): every eigenvalue within 1e-10 of the
+    FP64 golden values, and the largest residual at least halved against
+    polish off."""
+    from normalmodes_gb300.nmgpu import Solver, NM_PREC_MIXED
+    d = small_models[name]
+    g = _golden(name)
+    lo, hi = g["interval"]
+    out = {}
+    for pol in (-1, 0):
+        with Solver(d["mats"], d["porder"], precision=NM_PREC_MIXED, b_bounds=tuple(g["b_bounds"]),
+                    ap_bounds=tuple(g["ap_bounds"])) as sv:
+            out[pol] = sv.solve(lo, hi, ab_bounds=(float(g["xintv"][2]), float(g["xintv"][3])), block=32,
+                                polish=pol)
+    for pol, res in out.items():
+        assert len(res.lam) == len(g["lam"])
+    rel = np.abs(out[0].lam - g["lam"]) / g["lam"]
+    print(f"{name}: polished eigenvalue rel err max {rel.max():.2e}, err_ref max {out[0].err_ref.max():.2e} "
+          f"(unpolished {out[-1].err_ref.max():.2e})")
+    assert rel.max() <= 1e-10
+    assert out[0].err_ref.max() <= 0.5 * out[-1].err_ref.max()
