@@ -334,6 +334,8 @@ def main():
     spmv["filter_degree_step_ms"] = round(ms_f, 3)
     spmv["filter_degree_step_GBs"] = round(by_f / ms_f / 1e6, 1)
     winfo = warm.info()
+    tuned = {"mass": {"vector_gathers": winfo.mass_vec, "threads": winfo.mass_threads},
+             "ap": {"vector_gathers": winfo.ap_vec, "threads": winfo.ap_threads}}
 
     cpu = None
     if rank == 0 and not a.no_cpu:
@@ -358,7 +360,7 @@ def main():
                    "max_err_ref": float(res.err_ref.max()) if len(res.lam) else None,
                    "median_err_ref": float(np.median(res.err_ref)) if len(res.lam) else None,
                    "max_res2": float(res.res2.max()) if len(res.lam) else None,
-                   "parallelism": f"replicas x{ws}"},
+                   "parallelism": f"replicas x{ws}", "autotuned_gathers": tuned},
         "gpu_launches": kernels,
         "clocks": clocks,
         "roofline": roof,

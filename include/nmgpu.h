@@ -212,6 +212,9 @@ typedef struct {
   double t_setup;        /* seconds spent in nm_create                        */
   long long h2d_bytes;   /* bytes copied host -> device by nm_create          */
   size_t device_bytes;   /* device memory held by the context                 */
+  /* launch shape of the block filter's mass and Ap Chebyshev gathers picked
+   * by the autotuner (vec 1: 16-byte gathers; -1 before the first block use) */
+  int mass_vec, mass_threads, ap_vec, ap_threads;
 } nm_info;
 int nm_get_info(nm_ctx* ctx, nm_info* info);
 void* nm_get_stream(nm_ctx* ctx); /* cudaStream_t of the context */

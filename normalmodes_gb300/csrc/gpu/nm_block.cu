@@ -907,13 +907,17 @@ bool gather_vec(int nc) {
 }
 
 template <typename VT, typename XT, int NC>
-void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s) {
+void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s,
+                 const GatherCfg& cfg) {
   const int ng = M.nrows;
   if (ng == 0 || ch.deg == 0) return;
   const size_t len = (size_t)NC * ng * kBlk;
   XT* buf[2] = {work, work + len};  // x_j lives in buf[j & 1]
   const XT it = (XT)ch.inv_theta;
-  const int thr = gather_threads(), rows = thr / 32;
+  const bool vec = cfg.vec < 0 ? gather_vec(NC) : cfg.vec != 0;
+  const int thr = std::getenv("NM_GATHER_THREADS") ? gather_threads()
+                                                    : std::min(kT, std::max(32, cfg.threads / 32 * 32));
+  const int rows = thr / 32;
   const int grid = (ng + rows - 1) / rows;
   for (int j = 1; j <= ch.deg; ++j) {
     const XT a = (XT)ch.a[j - 1], c = (XT)ch.c[j - 1];
@@ -924,7 +928,7 @@ void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT*
   k_gcheb<VT, XT, NC, MODE><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it)
 #define NM_MC(MODE) \
   k_mass_cheb<VT, XT, NC, MODE><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it)
-    if (gather_vec(NC)) {
+    if (vec) {
       if (j == 1) NM_MV(0);
       else if (j == 2) NM_MV(1);
       else NM_MV(2);
@@ -940,13 +944,15 @@ void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT*
 }
 
 template <typename VT, typename XT>
-void blk_mass_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s) {
-  gather_cheb<VT, XT, 3>(M, ch, b, x, work, s);
+void blk_mass_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s,
+                   const GatherCfg& cfg) {
+  gather_cheb<VT, XT, 3>(M, ch, b, x, work, s, cfg);
 }
 
 template <typename VT, typename XT>
-void blk_ap_cheb(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s) {
-  gather_cheb<VT, XT, 1>(Ap, ch, b, x, work, s);
+void blk_ap_cheb(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s,
+                 const GatherCfg& cfg) {
+  gather_cheb<VT, XT, 1>(Ap, ch, b, x, work, s, cfg);
 }
 
 void blk_prefer_l1() {
@@ -1214,8 +1220,10 @@ void blk_init_filter(XT* vk, XT* vkm1, XT* y, const XT* v, double mu0, size_t le
 }
 
 #define NM_INST(VT, XT)                                                                                              \
-  template void blk_mass_cheb<VT, XT>(const GCsr<VT>&, const ChebSetup&, const XT*, XT*, XT*, cudaStream_t);        \
-  template void blk_ap_cheb<VT, XT>(const GCsr<VT>&, const ChebSetup&, const XT*, XT*, XT*, cudaStream_t);          \
+  template void blk_mass_cheb<VT, XT>(const GCsr<VT>&, const ChebSetup&, const XT*, XT*, XT*, cudaStream_t,          \
+                                      const GatherCfg&);                                                           \
+  template void blk_ap_cheb<VT, XT>(const GCsr<VT>&, const ChebSetup&, const XT*, XT*, XT*, cudaStream_t,            \
+                                    const GatherCfg&);                                                             \
   template void blk_et<VT, XT>(const GCsr<VT>&, const XT*, XT*, cudaStream_t);                                     \
   template void blk_ap_cheb_persistent<VT, XT>(const GCsr<VT>&, const ChebSetup&, const XT*, XT*, XT*, GridBar*,   \
                                                int*, int, cudaStream_t);                                           \

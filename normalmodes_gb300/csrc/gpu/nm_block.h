@@ -86,11 +86,22 @@ int upload_g(nm_ctx* c, const GCsrHost& h, GCsr<T>& d);
 template <typename T>
 void free_g(GCsr<T>& g);
 
+// Launch shape of the gather Chebyshev kernels: vec 1 = 16-byte vector
+// gathers (k_gcheb), 0 = one value per lane (k_mass_cheb), -1 = the default
+// for the component count; threads per CTA (one row per warp).  Picked per
+// context by the autotuner (block_autotune).
+struct GatherCfg {
+  int vec = -1;
+  int threads = 256;
+};
+
 // Block kernels (S = kBlk columns, row-major blocks).
 template <typename VT, typename XT>
-void blk_mass_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s);
+void blk_mass_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s,
+                   const GatherCfg& cfg = GatherCfg());
 template <typename VT, typename XT>
-void blk_ap_cheb(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s);
+void blk_ap_cheb(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s,
+                 const GatherCfg& cfg = GatherCfg());
 // Prefer L1 over shared memory for the gather kernels (once per context).
 void blk_prefer_l1();
 template <typename VT, typename XT>
@@ -159,12 +170,18 @@ struct BlockState {
   // Chebyshev set-ups of the FP32 filter's inner solves (degrees matched to
   // FP32 accuracy; mixed path only, set by block_buffers)
   ChebSetup chB32, chAp32;
+  // launch shapes of the gather solves chosen by block_autotune
+  GatherCfg gm32, gm64, ga32, ga64;
+  bool tuned = false;
   size_t f32_len = 0, f64_len = 0;
   cublasHandle_t cublas = nullptr;
   cusolverDnHandle_t cusolver = nullptr;
   int coop = 0;
 };
 int block_buffers(nm_ctx* c);
+// Times the gather-kernel variants of the mass and Ap Chebyshev solves on
+// this context's matrices and keeps the fastest (once per context).
+int block_autotune(nm_ctx* c);
 int block_time_op(nm_ctx* c, int which, int reps, double* ms, double* bytes, int* launches_per_op);
 int block_build(nm_ctx* c, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, const nm_csr* E, const nm_csr* ET);
 void block_free(nm_ctx* c);

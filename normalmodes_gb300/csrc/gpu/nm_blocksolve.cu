@@ -195,7 +195,8 @@ void blk_mass_solve(nm_ctx* c, const GCsr<VT>& M, const XT* b, XT* x, XT* work) 
       return;
     }
   }
-  blk_mass_cheb<VT, XT>(M, mass_cheb<XT>(c), b, x, work, c->stream);
+  blk_mass_cheb<VT, XT>(M, mass_cheb<XT>(c), b, x, work, c->stream,
+                        std::is_same<XT, float>::value ? st->gm32 : st->gm64);
 }
 template <typename VT, typename XT>
 void blk_ap_solve(nm_ctx* c, const GCsr<VT>& Ap, const XT* b, XT* x, XT* work) {
@@ -210,7 +211,8 @@ void blk_ap_solve(nm_ctx* c, const GCsr<VT>& Ap, const XT* b, XT* x, XT* work) {
   if (kind == 2 && st->coop > 0)  // the persistent kernel reads the reference set-up's device coefficients
     blk_ap_cheb_persistent<VT, XT>(Ap, c->chebAp, b, x, work, c->bar, c->d_status, st->coop, c->stream);
   else
-    blk_ap_cheb<VT, XT>(Ap, ap_cheb<XT>(c), b, x, work, c->stream);
+    blk_ap_cheb<VT, XT>(Ap, ap_cheb<XT>(c), b, x, work, c->stream,
+                        std::is_same<XT, float>::value ? st->ga32 : st->ga64);
 }
 
 // Degree at which the Chebyshev semi-iteration on [lmin, lmax] reaches the
@@ -321,6 +323,76 @@ double filter_at_zero(const Pol& pol) {
 
 }  // namespace
 
+int block_autotune(nm_ctx* c) {
+  BlockState* st = bs(c);
+  if (!st || !st->ok || st->tuned) return NM_OK;
+  st->tuned = true;
+  if (std::getenv("NM_GATHER_VEC") || std::getenv("NM_GATHER_THREADS")) return NM_OK;  // fixed by hand
+  if (const char* e = std::getenv("NM_AUTOTUNE"))
+    if (std::atoi(e) == 0) return NM_OK;
+  const int n = c->n, np = c->np;
+  const bool mixed = c->precision == NM_PREC_MIXED;
+  const size_t L = (size_t)kBlk * n, P = (size_t)kBlk * (np ? np : 1);
+  cudaStream_t s = c->stream;
+  cudaEvent_t e0, e1;
+  NM_CUDA(c, cudaEventCreate(&e0));
+  NM_CUDA(c, cudaEventCreate(&e1));
+  const GatherCfg cands[4] = {{0, 256}, {1, 256}, {0, 128}, {1, 128}};
+  // time one solve (after one untimed run) for every candidate; keep the fastest
+  auto pick = [&](auto&& run, GatherCfg& best) -> int {
+    float tbest = 1e30f;
+    for (const GatherCfg& g : cands) {
+      run(g);
+      NM_CUDA(c, cudaEventRecord(e0, s));
+      run(g);
+      run(g);
+      NM_CUDA(c, cudaEventRecord(e1, s));
+      NM_CUDA(c, cudaEventSynchronize(e1));
+      float ms = 0.f;
+      NM_CUDA(c, cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < tbest) {
+        tbest = ms;
+        best = g;
+      }
+    }
+    return NM_OK;
+  };
+  int rc;
+  if (mixed) {
+    float* p = st->f32;  // scratch: the FP32 filter buffers (zeroed)
+    NM_CUDA(c, cudaMemsetAsync(p, 0, sizeof(float) * (6 * L), s));
+    const ChebSetup& chB = st->chB32.deg > 0 ? st->chB32 : c->chebB;
+    if ((rc = pick([&](const GatherCfg& g) { blk_mass_cheb<float, float>(st->M32, chB, p, p + L, p + 2 * L, s, g); },
+                   st->gm32)))
+      return rc;
+    if (c->fs) {
+      const ChebSetup& chA = st->chAp32.deg > 0 ? st->chAp32 : c->chebAp;
+      if ((rc = pick([&](const GatherCfg& g) { blk_ap_cheb<float, float>(st->Ap32, chA, p, p + P, p + 2 * P, s, g); },
+                     st->ga32)))
+        return rc;
+    }
+  }
+  {
+    double* p = st->f64;  // scratch: the FP64 block buffers (zeroed)
+    NM_CUDA(c, cudaMemsetAsync(p, 0, sizeof(double) * (6 * L), s));
+    if ((rc = pick([&](const GatherCfg& g) {
+           blk_mass_cheb<double, double>(st->M64, c->chebB, p, p + L, p + 2 * L, s, g);
+         }, st->gm64)))
+      return rc;
+    if (c->fs && (rc = pick([&](const GatherCfg& g) {
+                    blk_ap_cheb<double, double>(st->Ap64, c->chebAp, p, p + P, p + 2 * P, s, g);
+                  }, st->ga64)))
+      return rc;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (c->verbose)
+    printf(" autotune: mass fp32 vec %d x %d, fp64 vec %d x %d; Ap fp32 vec %d x %d, fp64 vec %d x %d\n",
+           st->gm32.vec, st->gm32.threads, st->gm64.vec, st->gm64.threads, st->ga32.vec, st->ga32.threads,
+           st->ga64.vec, st->ga64.threads);
+  return NM_OK;
+}
+
 int block_buffers(nm_ctx* c) {
   BlockState* st = bs(c);
   if (!st || !st->ok) return set_err(c, NM_ERR_ARG, "block mode needs the 3-component operator structure");
@@ -368,7 +440,7 @@ int block_buffers(nm_ctx* c) {
     st->f64_len = need64;
     c->dev_bytes += need64 * 8;
   }
-  return NM_OK;
+  return block_autotune(c);
 }
 
 // Timing of the block operators (CUDA events on the context's stream).
@@ -580,7 +652,7 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   // FP64 block B~^-1: col-major (ld ldw) in -> col-major out
   auto bsolve_blk = [&](const double* in, size_t ldin, double* out, size_t ldout) {
     blk_from_colmajor<double>(in, ldin, n, sin_, s);
-    blk_mass_cheb<double, double>(st->M64, c->chebB, sin_, sout, swork, s);
+    blk_mass_cheb<double, double>(st->M64, c->chebB, sin_, sout, swork, s, st->gm64);
     blk_to_colmajor<double>(sout, n, out, ldout, s);
     c->n_bsolve += S;
     c->n_spmv += c->chebB.deg;

@@ -292,6 +292,18 @@ int nm_get_info(nm_ctx* c, nm_info* info) {
   info->t_setup = c->t_setup;
   info->h2d_bytes = c->h2d_bytes;
   info->device_bytes = c->dev_bytes;
+  info->mass_vec = info->mass_threads = info->ap_vec = info->ap_threads = -1;
+  if (const nmg::BlockState* st = (const nmg::BlockState*)c->blk) {
+    if (st->tuned) {
+      const bool mixed = c->precision == NM_PREC_MIXED;
+      const nmg::GatherCfg& gm = mixed ? st->gm32 : st->gm64;
+      const nmg::GatherCfg& ga = mixed ? st->ga32 : st->ga64;
+      info->mass_vec = gm.vec;
+      info->mass_threads = gm.threads;
+      info->ap_vec = ga.vec;
+      info->ap_threads = ga.threads;
+    }
+  }
   return NM_OK;
 }
 

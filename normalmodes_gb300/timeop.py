@@ -43,6 +43,9 @@ def main(argv=None) -> None:
             ms, by, la = sv.time_op(w, a.reps)
             out[str(w)] = {"ms": round(ms, 4), "GBs": round(by / ms / 1e6, 1), "launches": la,
                            "bytes": by}
+        i2 = sv.info()
+        out["autotuned"] = {"mass_vec": i2.mass_vec, "mass_threads": i2.mass_threads, "ap_vec": i2.ap_vec,
+                            "ap_threads": i2.ap_threads}
     print(json.dumps(out))
 
 
