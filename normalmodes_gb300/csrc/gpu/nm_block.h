@@ -193,12 +193,15 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
 // (U^T A U) Q = (U^T B U) Q Theta.  Resolves the mixing of close Ritz pairs
 // left by an FP32 filter.
 int rayleigh_ritz64(nm_ctx* c, double** U, int nc, std::vector<double>* theta = nullptr);
-// Mixed path: refine the Ritz vectors U (n x nc, B-normalised, Ritz values
-// theta) towards FP64 accuracy: U <- U + B~^-1 D / tau, the part of
-// q(A B~^-1) B U that differs from q(theta) B U, with q the degree-deg
-// Chebyshev polynomial of [cfrac lmax, lmax].  D follows the three-term
-// recurrence driven by the FP64 residual A U - theta B U and runs in FP32
-// (it is small, so FP32 rounding stays at FP64 level relative to U).
-int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, int deg, double cfrac);
+// Mixed path: refine the Ritz vectors U (n x nc, B-normalised, ascending
+// Ritz values theta) towards FP64 accuracy: U <- U + B~^-1 D / tau, the
+// part of q(A B~^-1) B U that differs from q(theta) B U, with q a Chebyshev
+// polynomial of [c lmax, lmax] whose degree falls from deg for the lowest
+// Ritz values to 20 as sqrt(theta_0 / theta) (c = max(25 / degree^2,
+// bfloor); cfrac <= 0 disables the degree fall-off).  D follows the
+// three-term recurrence driven by the FP64 residual A U - theta B U and runs
+// in FP32 (it is small, so FP32 rounding stays at FP64 level relative to U).
+int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, int deg, double cfrac,
+             double bfloor);
 
 }  // namespace nmg

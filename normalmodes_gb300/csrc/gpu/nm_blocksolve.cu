@@ -1044,7 +1044,8 @@ int rayleigh_ritz64(nm_ctx* c, double** Uio, int nc, std::vector<double>* theta)
   return NM_OK;
 }
 
-int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, int deg, double cfrac) {
+int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, int deg, double cfrac,
+             double bfloor) {
   BlockState* st = bs(c);
   if (!st || !st->ok || nc <= 0 || deg <= 0 || c->precision != NM_PREC_MIXED) return NM_OK;
   if ((int)theta.size() < nc || !(lmax > 0.0) || !(cfrac > 0.0 && cfrac < 1.0))
@@ -1064,8 +1065,12 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
   double* y0 = carve(p64, P);
   double* apw = carve(p64, 4 * P);
   FiltBufs<float> f = filt_carve<float>(st->f32, n, np);
-  // polynomial q = T_deg(l(x)), l(x) = alpha x - beta maps [c0, lmax] to [-1, 1]
-  const double c0 = cfrac * lmax, alpha = 2.0 / (lmax - c0), beta = (lmax + c0) / (lmax - c0);
+  // Per block of 32 Ritz vectors (ascending theta): degree deg for the
+  // lowest values, falling as sqrt(theta_0 / theta) to a floor of 20 (the
+  // eigenvalue error of a mode grows with lmax / theta, so higher modes need
+  // less damping); the band starts at max(25 / deg^2, bfloor) lmax.
+  const double th0 = nc > 0 && theta[0] > 0.0 ? theta[0] : 0.0;
+  const int dfloor = std::min(deg, 20);
   double *Up = nullptr, *dth = nullptr, *dsc = nullptr;
   float* dfor = nullptr;
   auto release = [&]() {
@@ -1085,15 +1090,27 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
   NM_CUDA(c, cudaMemsetAsync(Up, 0, nb, s));
   NM_CUDA(c, cudaMemcpyAsync(Up, U, sizeof(double) * (size_t)n * nc, cudaMemcpyDeviceToDevice, s));
   FiltEpi ep0;  // plain product
-  FiltEpi ep;   // D_{j+1} = 2 alpha A B~^-1 D_j - 2 beta D_j - D_{j-1}
-  ep.mode = 1;
-  ep.s = 2.0 * alpha;
-  ep.cc = beta / alpha;
-  ep.pm = 1.0;
-  ep.mu = 0.0;
   std::vector<double> th(S), sc(S);
   std::vector<float> forc((size_t)S * deg);
+  long long steps = 0;
   for (int j0 = 0; j0 < ncp; j0 += S) {
+    int dblk = deg;
+    if (th0 > 0.0 && cfrac > 0.0) {
+      const double r = theta[j0] > th0 ? std::sqrt(th0 / theta[j0]) : 1.0;
+      dblk = std::max(dfloor, std::min(deg, (int)std::lround(deg * r)));
+    }
+    const double cf = std::max(25.0 / ((double)dblk * dblk), bfloor);
+    if (!(cf < 0.5)) continue;
+    // polynomial q = T_dblk(l(x)), l(x) = alpha x - beta maps [c0, lmax] to [-1, 1]
+    const double c0 = cf * lmax, alpha = 2.0 / (lmax - c0), beta = (lmax + c0) / (lmax - c0);
+    FiltEpi ep;  // D_{j+1} = 2 alpha A B~^-1 D_j - 2 beta D_j - D_{j-1}
+    ep.mode = 1;
+    ep.s = 2.0 * alpha;
+    ep.cc = beta / alpha;
+    ep.pm = 1.0;
+    ep.mu = 0.0;
+    const int deg = dblk;  // this block's degree
+    steps += deg;
     // per-column scalars: tau_j = T_j(l(theta)), forcing 2 alpha tau_j
     for (int col = 0; col < S; ++col) {
       const double t = j0 + col < nc ? theta[j0 + col] : 0.0;
@@ -1144,7 +1161,7 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
     blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
     blk_add_colmajor(f.w2, dsc, n, Up + (size_t)j0 * n, n, s);
   }
-  c->n_amv += (long long)ncp * deg;
+  c->n_amv += steps * S;
   NM_CUDA(c, cudaMemcpyAsync(U, Up, sizeof(double) * (size_t)n * nc, cudaMemcpyDeviceToDevice, s));
   NM_CUDA(c, cudaGetLastError());
   release();

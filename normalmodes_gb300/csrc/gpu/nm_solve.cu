@@ -440,7 +440,8 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
         // Ritz value lies below the band
         const double cfrac = std::max(25.0 / ((double)pdeg * pdeg), 2.0 * ib / lmax);
         if (cfrac < 0.5) {
-          if ((rc = polish64(c, U, nc, theta, lmax, pdeg, cfrac)) || (rc = rayleigh_ritz64(c, &U, nc))) {
+          if ((rc = polish64(c, U, nc, theta, lmax, pdeg, cfrac, 2.0 * ib / lmax)) ||
+              (rc = rayleigh_ritz64(c, &U, nc))) {
             cudaFree(U);
             return rc;
           }
