@@ -215,6 +215,7 @@ int nm_adjoint(nm_ctx* c, const nm_elem_model* em, int k, const double* lam, con
     for (void* p : owned) cudaFree(p);
     owned.clear();
   };
+  auto guard = on_exit(release);
   int *d_tets, *d_vstt, *d_rnum, *d_pstt = nullptr;
   double *d_xyz, *d_lamf, *d_M, *d_D;
   unsigned char* d_fluid;

@@ -192,7 +192,9 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
 // FP64 Rayleigh-Ritz on the columns of U (n x nc): U <- U Q with
 // (U^T A U) Q = (U^T B U) Q Theta.  Resolves the mixing of close Ritz pairs
 // left by an FP32 filter.
-int rayleigh_ritz64(nm_ctx* c, double** U, int nc, std::vector<double>* theta = nullptr);
+// fp32_gemm: the three n x nc x nc products in FP32 (the pass before the
+// refinement, which only needs FP32-accurate Ritz vectors and values).
+int rayleigh_ritz64(nm_ctx* c, double** U, int nc, std::vector<double>* theta = nullptr, bool fp32_gemm = false);
 // Mixed path: refine the Ritz vectors U (n x nc, B-normalised, ascending
 // Ritz values theta) towards FP64 accuracy: U <- U + B~^-1 D / tau, the
 // part of q(A B~^-1) B U that differs from q(theta) B U, with q a Chebyshev

@@ -965,7 +965,7 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   return NM_OK;
 }
 
-int rayleigh_ritz64(nm_ctx* c, double** Uio, int nc, std::vector<double>* theta) {
+int rayleigh_ritz64(nm_ctx* c, double** Uio, int nc, std::vector<double>* theta, bool fp32_gemm) {
   BlockState* st = bs(c);
   if (!st || !st->ok || !st->cublas || nc <= 0) return NM_OK;
   const int n = c->n, np = c->np, S = kBlk;
@@ -984,15 +984,14 @@ int rayleigh_ritz64(nm_ctx* c, double** Uio, int nc, std::vector<double>* theta)
   double *Up = nullptr, *AU = nullptr, *BU = nullptr, *GA = nullptr, *GB = nullptr, *W = nullptr, *work = nullptr;
   int* info = nullptr;
   auto release = [&]() {
-    cudaFree(Up);
-    cudaFree(AU);
-    cudaFree(BU);
-    cudaFree(GA);
-    cudaFree(GB);
-    cudaFree(W);
-    cudaFree(work);
+    for (double** q : {&Up, &AU, &BU, &GA, &GB, &W, &work}) {
+      cudaFree(*q);
+      *q = nullptr;
+    }
     cudaFree(info);
+    info = nullptr;
   };
+  auto guard = on_exit(release);
   const size_t nb = sizeof(double) * (size_t)n * ncp;
   if (cudaMalloc(&Up, nb) != cudaSuccess || cudaMalloc(&AU, nb) != cudaSuccess || cudaMalloc(&BU, nb) != cudaSuccess ||
       cudaMalloc(&GA, sizeof(double) * (size_t)nc * nc) != cudaSuccess ||
@@ -1018,8 +1017,37 @@ int rayleigh_ritz64(nm_ctx* c, double** Uio, int nc, std::vector<double>* theta)
   c->n_amv += ncp;
   c->n_spmv += (long long)(ncp / S) * (c->fs ? 3 + c->chebAp.deg : 2);
   const double one = 1.0, zero = 0.0;
-  CB(c, cublasDgemm(st->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nc, nc, n, &one, Up, n, AU, n, &zero, GA, nc));
-  CB(c, cublasDgemm(st->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nc, nc, n, &one, Up, n, BU, n, &zero, GB, nc));
+  const float onef = 1.0f, zerof = 0.0f;
+  // FP32 copies for the three n x nc x nc products when fp32_gemm
+  float *U32 = nullptr, *AU32 = nullptr, *BU32 = nullptr, *G32 = nullptr;
+  auto release32 = [&]() {
+    for (float** q : {&U32, &AU32, &BU32, &G32}) {
+      cudaFree(*q);
+      *q = nullptr;
+    }
+  };
+  auto guard32 = on_exit(release32);
+  if (fp32_gemm) {
+    const size_t nb32 = sizeof(float) * (size_t)n * nc;
+    if (cudaMalloc(&U32, nb32) != cudaSuccess || cudaMalloc(&AU32, nb32) != cudaSuccess ||
+        cudaMalloc(&BU32, nb32) != cudaSuccess || cudaMalloc(&G32, sizeof(float) * (size_t)nc * nc) != cudaSuccess) {
+      cudaGetLastError();
+      release32();
+      fp32_gemm = false;  // not enough memory for the copies: FP64 products
+    }
+  }
+  if (fp32_gemm) {
+    blk_d2f(Up, n, U32, n, n, nc, s);
+    blk_d2f(AU, n, AU32, n, n, nc, s);
+    blk_d2f(BU, n, BU32, n, n, nc, s);
+    CB(c, cublasSgemm(st->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nc, nc, n, &onef, U32, n, AU32, n, &zerof, G32, nc));
+    blk_f2d(G32, nc, GA, nc, nc, nc, s);
+    CB(c, cublasSgemm(st->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nc, nc, n, &onef, U32, n, BU32, n, &zerof, G32, nc));
+    blk_f2d(G32, nc, GB, nc, nc, nc, s);
+  } else {
+    CB(c, cublasDgemm(st->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nc, nc, n, &one, Up, n, AU, n, &zero, GA, nc));
+    CB(c, cublasDgemm(st->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nc, nc, n, &one, Up, n, BU, n, &zero, GB, nc));
+  }
   int lw = 0;
   CS(c, cusolverDnDsygvd_bufferSize(st->cusolver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
                                     CUBLAS_FILL_MODE_LOWER, nc, GA, nc, GB, nc, W, &lw));
@@ -1034,7 +1062,13 @@ int rayleigh_ritz64(nm_ctx* c, double** Uio, int nc, std::vector<double>* theta)
     return set_err(c, NM_ERR_NUMERIC, "Rayleigh-Ritz generalized eigensolve failed");
   }
   // U <- U Q  (Q in GA, B-orthonormal columns)
-  CB(c, cublasDgemm(st->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, nc, nc, &one, Up, n, GA, nc, &zero, U, n));
+  if (fp32_gemm) {
+    blk_d2f(GA, nc, G32, nc, nc, nc, s);
+    CB(c, cublasSgemm(st->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, nc, nc, &onef, U32, n, G32, nc, &zerof, AU32, n));
+    blk_f2d(AU32, n, U, n, n, nc, s);
+  } else {
+    CB(c, cublasDgemm(st->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, nc, nc, &one, Up, n, GA, nc, &zero, U, n));
+  }
   if (theta) {
     theta->resize(nc);
     NM_CUDA(c, cudaMemcpyAsync(theta->data(), W, sizeof(double) * nc, cudaMemcpyDeviceToHost, s));
@@ -1075,11 +1109,14 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
   float* dfor = nullptr;
   auto release = [&]() {
     cudaStreamSynchronize(s);
-    cudaFree(Up);
-    cudaFree(dth);
-    cudaFree(dsc);
+    for (double** q : {&Up, &dth, &dsc}) {
+      cudaFree(*q);
+      *q = nullptr;
+    }
     cudaFree(dfor);
+    dfor = nullptr;
   };
+  auto guard = on_exit(release);
   const size_t nb = sizeof(double) * (size_t)n * ncp;
   if (cudaMalloc(&Up, nb) != cudaSuccess || cudaMalloc(&dth, sizeof(double) * S) != cudaSuccess ||
       cudaMalloc(&dsc, sizeof(double) * S) != cudaSuccess ||

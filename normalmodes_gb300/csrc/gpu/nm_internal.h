@@ -122,6 +122,17 @@ namespace nmg {
 long long launches();
 void add_launches(long long k);
 
+// Runs f when the scope ends (device scratch released on every return path).
+template <typename F>
+struct OnExit {
+  F f;
+  ~OnExit() { f(); }
+};
+template <typename F>
+OnExit<F> on_exit(F f) {
+  return OnExit<F>{f};
+}
+
 // ---------------------------------------------------------------- status
 int set_err(nm_ctx* c, int code, const std::string& msg);
 #define NM_CUDA(c, call)                                                                 \
