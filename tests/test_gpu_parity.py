@@ -3,8 +3,8 @@ FP64 oracle (oracle/) on the same synthetic models.
 
 Tolerances (FP64 path): operators 1e-12 relative in the max norm (the GPU
 sums each row in CSR order with FMA; the oracle without), eigenvalues 1e-10
-relative (the BASELINE target), identical eigenvalue counts, and the
-reference's RMS residual (src/mod_pevsl.f90:158) below 1e-10.
+relative, identical eigenvalue counts, and the reference's RMS residual
+(src/mod_pevsl.f90:158) below 1e-10.
 """
 import numpy as np
 import pytest
