@@ -195,6 +195,33 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
 // fp32_gemm: the three n x nc x nc products in FP32 (the pass before the
 // refinement, which only needs FP32-accurate Ritz vectors and values).
 int rayleigh_ritz64(nm_ctx* c, double** U, int nc, std::vector<double>* theta = nullptr, bool fp32_gemm = false);
+// Plan of the mixed path's refinement for the interval xintv = [a, b,
+// lmin, lmax] and a requested degree (0: default 80, < 0: off).  Any
+// polynomial that damps the upper spectrum grows below theta: the
+// components of a Ritz vector along the lower wanted modes and the zero
+// modes are amplified by about exp(deg^2 (b - a) / (5 lmax)) when the band
+// starts at c = 25 lmax / deg^2, so the degree is capped at
+// 2 sqrt(lmax / (b - a)) (growth below ~2).  The band [c, lmax] is damped by
+// ~1e4 (deg acosh(1 + 2 c / lmax) ~ 10) and starts above the interval with
+// a margin (c >= 2 b = bfloor lmax), so every Ritz value lies below it.
+struct PolishPlan {
+  int deg = 0;          // degree for the lowest Ritz values (0: no refinement)
+  double cfrac = 1.0;   // band start / lmax at that degree
+  double bfloor = 1.0;  // lower limit of the band start: 2 b / lmax
+  bool refine = false;
+};
+PolishPlan polish_plan(const double xintv[4], int requested);
+// Degree of one block of Ritz values starting at theta (theta0 the lowest):
+// deg sqrt(theta0 / theta), clamped to [min(20, deg), deg].
+int polish_block_degree(const PolishPlan& p, double theta0, double theta);
+// Band start / lmax for a block of degree d: max(25 / d^2, bfloor).
+double polish_band(const PolishPlan& p, int d);
+// Chebyshev degree reaching relative error eps on [lmin, lmax] of ref
+// (2 sigma^d <= eps), never above ref.deg.
+int cheb_degree_for(const ChebSetup& ref, double eps);
+// p(0) of a filter polynomial: sum_k mu_k T_k(-cc / dd).
+double filter_at_zero(const Pol& pol);
+
 // Mixed path: refine the Ritz vectors U (n x nc, B-normalised, ascending
 // Ritz values theta) towards FP64 accuracy: U <- U + B~^-1 D / tau, the
 // part of q(A B~^-1) B U that differs from q(theta) B U, with q a Chebyshev
@@ -203,7 +230,6 @@ int rayleigh_ritz64(nm_ctx* c, double** U, int nc, std::vector<double>* theta = 
 // bfloor); cfrac <= 0 disables the degree fall-off).  D follows the
 // three-term recurrence driven by the FP64 residual A U - theta B U and runs
 // in FP32 (it is small, so FP32 rounding stays at FP64 level relative to U).
-int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, int deg, double cfrac,
-             double bfloor);
+int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, const PolishPlan& plan);
 
 }  // namespace nmg

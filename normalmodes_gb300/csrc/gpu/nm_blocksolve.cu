@@ -215,17 +215,6 @@ void blk_ap_solve(nm_ctx* c, const GCsr<VT>& Ap, const XT* b, XT* x, XT* work) {
                         std::is_same<XT, float>::value ? st->ga32 : st->ga64);
 }
 
-// Degree at which the Chebyshev semi-iteration on [lmin, lmax] reaches the
-// relative error eps: 2 sigma^d <= eps, sigma = (sqrt(k) - 1) / (sqrt(k) + 1),
-// k = lmax / lmin (Golub & Varga); never above the reference's degree.
-int cheb_degree_for(const ChebSetup& ref, double eps) {
-  if (!(ref.lmin > 0.0) || !(ref.lmax > ref.lmin)) return ref.deg;
-  const double k = ref.lmax / ref.lmin, sk = std::sqrt(k);
-  const double sigma = (sk - 1.0) / (sk + 1.0);
-  if (!(sigma > 0.0)) return std::min(ref.deg, 1);
-  const int d = (int)std::ceil(std::log(eps / 2.0) / std::log(sigma));
-  return std::max(1, std::min(ref.deg, d));
-}
 
 template <typename VT, typename XT>
 void block_filter(nm_ctx* c, const Pol& pol, const GCsr<VT>& M, const GCsr<VT>& A, const GCsr<VT>& Ap,
@@ -308,7 +297,22 @@ void block_filter_range(nm_ctx* c, const Pol& pol, FiltBufs<float> f, double* si
   blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin64, y064, sout64, nullptr, nullptr, nullptr, ep0, s);
 }
 
-// p(0) of the filter polynomial: sum_k mu_k T_k(-cc/dd).
+
+}  // namespace
+
+// Degree at which the Chebyshev semi-iteration on [lmin, lmax] reaches the
+// relative error eps: 2 sigma^d <= eps, sigma = (sqrt(k) - 1) / (sqrt(k) + 1),
+// k = lmax / lmin (Golub & Varga); never above the reference's degree.
+int cheb_degree_for(const ChebSetup& ref, double eps) {
+  if (!(ref.lmin > 0.0) || !(ref.lmax > ref.lmin)) return ref.deg;
+  const double k = ref.lmax / ref.lmin, sk = std::sqrt(k);
+  const double sigma = (sk - 1.0) / (sk + 1.0);
+  if (!(sigma > 0.0)) return std::min(ref.deg, 1);
+  const int d = (int)std::ceil(std::log(eps / 2.0) / std::log(sigma));
+  return std::max(1, std::min(ref.deg, d));
+}
+
+// p(0) of a filter polynomial: sum_k mu_k T_k(-cc/dd).
 double filter_at_zero(const Pol& pol) {
   const double l0 = -pol.cc / pol.dd;
   double tkm1 = 1.0, tk = l0, p0 = pol.mu.empty() ? 0.0 : pol.mu[0];
@@ -321,7 +325,30 @@ double filter_at_zero(const Pol& pol) {
   return p0;
 }
 
-}  // namespace
+PolishPlan polish_plan(const double xintv[4], int requested) {
+  PolishPlan p;
+  const double lmax = xintv[3], ia = std::max(xintv[0], 0.0), ib = xintv[1];
+  const int pcap = ib > ia && lmax > 0.0 ? (int)std::floor(2.0 * std::sqrt(lmax / (ib - ia))) : 0;
+  const int preq = requested < 0 ? 0 : requested == 0 ? 80 : requested;
+  const int d = std::min(preq, pcap);
+  if (d < 4) return p;
+  p.deg = d;
+  p.bfloor = 2.0 * ib / lmax;
+  p.cfrac = polish_band(p, d);
+  p.refine = p.cfrac < 0.5;
+  return p;
+}
+
+int polish_block_degree(const PolishPlan& p, double theta0, double theta) {
+  if (p.deg <= 0) return 0;
+  const int dfloor = std::min(p.deg, 20);
+  const double r = theta0 > 0.0 && theta > theta0 ? std::sqrt(theta0 / theta) : 1.0;
+  return std::max(dfloor, std::min(p.deg, (int)std::lround(p.deg * r)));
+}
+
+double polish_band(const PolishPlan& p, int d) {
+  return d > 0 ? std::max(25.0 / ((double)d * d), p.bfloor) : 1.0;
+}
 
 int block_autotune(nm_ctx* c) {
   BlockState* st = bs(c);
@@ -1078,12 +1105,11 @@ int rayleigh_ritz64(nm_ctx* c, double** Uio, int nc, std::vector<double>* theta,
   return NM_OK;
 }
 
-int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, int deg, double cfrac,
-             double bfloor) {
+int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, const PolishPlan& plan) {
+  const int deg = plan.deg;
   BlockState* st = bs(c);
   if (!st || !st->ok || nc <= 0 || deg <= 0 || c->precision != NM_PREC_MIXED) return NM_OK;
-  if ((int)theta.size() < nc || !(lmax > 0.0) || !(cfrac > 0.0 && cfrac < 1.0))
-    return set_err(c, NM_ERR_ARG, "polish: bad arguments");
+  if ((int)theta.size() < nc || !(lmax > 0.0) || !plan.refine) return set_err(c, NM_ERR_ARG, "polish: bad arguments");
   int rc;
   if ((rc = block_buffers(c))) return rc;
   const int n = c->n, np = c->np, S = kBlk;
@@ -1102,9 +1128,8 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
   // Per block of 32 Ritz vectors (ascending theta): degree deg for the
   // lowest values, falling as sqrt(theta_0 / theta) to a floor of 20 (the
   // eigenvalue error of a mode grows with lmax / theta, so higher modes need
-  // less damping); the band starts at max(25 / deg^2, bfloor) lmax.
+  // less damping); the band starts at polish_band(plan, degree) lmax.
   const double th0 = nc > 0 && theta[0] > 0.0 ? theta[0] : 0.0;
-  const int dfloor = std::min(deg, 20);
   double *Up = nullptr, *dth = nullptr, *dsc = nullptr;
   float* dfor = nullptr;
   auto release = [&]() {
@@ -1131,12 +1156,8 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
   std::vector<float> forc((size_t)S * deg);
   long long steps = 0;
   for (int j0 = 0; j0 < ncp; j0 += S) {
-    int dblk = deg;
-    if (th0 > 0.0 && cfrac > 0.0) {
-      const double r = theta[j0] > th0 ? std::sqrt(th0 / theta[j0]) : 1.0;
-      dblk = std::max(dfloor, std::min(deg, (int)std::lround(deg * r)));
-    }
-    const double cf = std::max(25.0 / ((double)dblk * dblk), bfloor);
+    const int dblk = polish_block_degree(plan, th0, theta[j0]);
+    const double cf = polish_band(plan, dblk);
     if (!(cf < 0.5)) continue;
     // polynomial q = T_dblk(l(x)), l(x) = alpha x - beta maps [c0, lmax] to [-1, 1]
     const double c0 = cf * lmax, alpha = 2.0 / (lmax - c0), beta = (lmax + c0) / (lmax - c0);
@@ -1206,3 +1227,34 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
 }
 
 }  // namespace nmg
+
+// ---------------------------------------------------------------- test hooks
+extern "C" {
+int nm_test_cheb_degree(double lmin, double lmax, int ref_deg, double eps) {
+  nmg::ChebSetup ch;
+  ch.lmin = lmin;
+  ch.lmax = lmax;
+  ch.deg = ref_deg;
+  return nmg::cheb_degree_for(ch, eps);
+}
+// p(0) of the filter find_pol designs for xintv (same arguments as nm_test_find_pol)
+double nm_test_filter_at_zero(const double* xintv, double thresh_int, double thresh_ext, int damping) {
+  const nmg::Pol P = nmg::find_pol(xintv, thresh_int, thresh_ext, 2, 10000, damping);
+  return nmg::filter_at_zero(P);
+}
+// refinement plan: out = {deg, refine}, band = {cfrac, bfloor}
+void nm_test_polish_plan(const double* xintv, int requested, int* out, double* band) {
+  const nmg::PolishPlan p = nmg::polish_plan(xintv, requested);
+  out[0] = p.deg;
+  out[1] = p.refine ? 1 : 0;
+  band[0] = p.cfrac;
+  band[1] = p.bfloor;
+}
+// per-block degree and band start of the plan for xintv / requested
+int nm_test_polish_block(const double* xintv, int requested, double theta0, double theta, double* band) {
+  const nmg::PolishPlan p = nmg::polish_plan(xintv, requested);
+  const int d = nmg::polish_block_degree(p, theta0, theta);
+  *band = nmg::polish_band(p, d);
+  return d;
+}
+}

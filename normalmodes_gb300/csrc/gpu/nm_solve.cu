@@ -419,20 +419,9 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
     // FP64 Rayleigh-Ritz over the Ritz block separates them.
     if (mixed) {
       // FP64-accurate refinement of the Ritz vectors between two
-      // Rayleigh-Ritz passes.  Any polynomial that damps the upper spectrum
-      // grows below theta: the components of a Ritz vector along the lower
-      // wanted modes and the zero modes are amplified by about
-      // exp(deg^2 (b - a) / (5 lmax)) when the band starts at
-      // c = 25 lmax / deg^2.  The degree is capped so that this stays below
-      // ~2 (deg <= 2 sqrt(lmax / (b - a))); the band [c, lmax] is damped by
-      // ~1e4 (deg * acosh(1 + 2 c / lmax) ~ 10) and starts above the
-      // interval with a margin (c >= 2 b), so every Ritz value lies below it.
-      const double lmax = res->xintv[3], ia = std::max(res->xintv[0], 0.0), ib = res->xintv[1];
-      const int pcap = ib > ia ? (int)std::floor(2.0 * std::sqrt(lmax / (ib - ia))) : 0;
-      const int preq = o.polish < 0 ? 0 : o.polish == 0 ? 80 : o.polish;
-      const int pdeg = std::min(preq, pcap) >= 4 ? std::min(preq, pcap) : 0;
-      const double cfrac = pdeg > 0 ? std::max(25.0 / ((double)pdeg * pdeg), 2.0 * ib / lmax) : 1.0;
-      const bool refine = pdeg > 0 && nc > 0 && cfrac < 0.5;
+      // Rayleigh-Ritz passes (plan: degree, band, see polish_plan)
+      const PolishPlan plan = polish_plan(res->xintv, o.polish);
+      const bool refine = plan.refine && nc > 0;
       std::vector<double> theta;
       // the first pass only feeds the refinement (FP32-accurate Ritz pairs
       // suffice, FP32 products); without refinement it is the FP64 pass
@@ -441,7 +430,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
         return rc;
       }
       if (refine) {
-        if ((rc = polish64(c, U, nc, theta, lmax, pdeg, cfrac, 2.0 * ib / lmax)) ||
+        if ((rc = polish64(c, U, nc, theta, res->xintv[3], plan)) ||
             (rc = rayleigh_ritz64(c, &U, nc))) {
           cudaFree(U);
           return rc;

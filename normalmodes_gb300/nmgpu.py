@@ -123,6 +123,13 @@ def lib() -> C.CDLL:
         L.nm_sync.argtypes = [vp]
         L.nm_time_op.argtypes = [vp, C.c_int, C.c_int, dp, dp, C.POINTER(C.c_int)]
         L.nm_test_barrier_timeout.argtypes = [vp, C.c_longlong]
+        L.nm_test_cheb_degree.argtypes = [C.c_double, C.c_double, C.c_int, C.c_double]
+        L.nm_test_cheb_degree.restype = C.c_int
+        L.nm_test_filter_at_zero.argtypes = [dp, C.c_double, C.c_double, C.c_int]
+        L.nm_test_filter_at_zero.restype = C.c_double
+        L.nm_test_polish_plan.argtypes = [dp, C.c_int, C.POINTER(C.c_int), dp]
+        L.nm_test_polish_block.argtypes = [dp, C.c_int, C.c_double, C.c_double, dp]
+        L.nm_test_polish_block.restype = C.c_int
         L.nm_solve_batched.argtypes = [vp, C.POINTER(NmSlice), C.c_int, C.POINTER(NmSolveOpts), C.POINTER(NmResult)]
         L.nm_adjoint.argtypes = [vp, C.POINTER(NmElemModel), C.c_int, dp, dp, C.c_int, C.c_int, C.c_double, dp,
                                  C.POINTER(C.c_int), C.POINTER(C.c_int)]
