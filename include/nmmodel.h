@@ -85,8 +85,28 @@ int nmm_ball_create(const nmm_ball_opts* o, nmm_model** out);
  * src/mod_cg_models.f90:301-364. */
 int nmm_load_files(const char* base_path, int porder, nmm_model** out);
 
-/* Assemble the CSR operators (JOB = 1: no gravity). */
+/* Assemble the CSR operators: JOB = 1 without gravity, JOB = 2 (reference
+ * gravity, src/mod_para.f90:133-138) once a gravity field is set. */
 int nmm_assemble(nmm_model* m);
+
+/* Reference gravity (JOB = 2): the gravitational acceleration at every
+ * element node, float64 Ntet x pNp x 3 in m/s^2 (pointing inwards), the
+ * layout of <base>_pod_<p>_potential_acceleration_true.dat
+ * (src/mod_cg_models.f90:366-429).  Copied; NULL switches gravity off
+ * (JOB = 1).  Either way the model is marked for re-assembly. */
+int nmm_set_gravity(nmm_model* m, const double* g0);
+
+/* Read <base>_pod_<p>_potential_acceleration_true.dat and set it. */
+int nmm_load_gravity(nmm_model* m, const char* base_path);
+
+/* Reference gravity of a generated ball from its radial density profile
+ * (the lateral perturbation has zero mean on every sphere):
+ * g = -G M(r) x / r^3, G in m^3 kg^-1 s^-2 (6.6723e-11 reproduces the
+ * reference's demo gravity files).  NMM_ERR_STATE for loaded models. */
+int nmm_ball_gravity(nmm_model* m, double G);
+
+/* The gravity field (borrowed, 3 pNp Ntet values) or NULL when off. */
+int nmm_get_gravity(const nmm_model* m, const double** g0);
 
 int nmm_info(const nmm_model* m, nmm_info_t* info);
 

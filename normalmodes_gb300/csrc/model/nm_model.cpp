@@ -1,5 +1,6 @@
 // Synthetic layered-ball models, the reference element and the CG mixed-FEM
-// assembly (JOB = 1) that produce the CSR operators of the eigensolve path.
+// assembly (JOB = 1, and JOB = 2 with the reference gravity) that produce the
+// CSR operators of the eigensolve path.
 //
 // The formulas follow the reference's assembly statement by statement:
 //   reference element   src/mod_geometry.f90:2307-2523 (nodes, MassM, Drst,
@@ -12,6 +13,8 @@
 //                       :279-452 (solid branch of CGFSE3D_ISO)
 //   fluid elements      src/mod_cg_create_matrix.f90:453-801
 //   f-s interface faces src/mod_cg_create_matrix.f90:803-953
+//   reference gravity   src/mod_cg_create_matrix.f90:192-265, 329-377,
+//                       492-608, 643-705, 866-920, 1057-1160 (JOB = 2)
 //   CSR structure       src/mod_cg_create_matrix.f90:1269-1455, 1458-2033
 //   node status         src/mod_geometry.f90:284-312, 672-680
 // The reference element is built from the exact Lagrange basis on the
@@ -378,6 +381,12 @@ struct nmm_model {
   std::vector<unsigned char> bface;  // 4*ntet: face on the outer boundary
   std::vector<int> vstat, rnum, pnum, vstt, pstt;
   std::vector<int> orig;  // per node: its id in the input numbering (vertices, then edge nodes)
+  // Reference gravity (JOB = 2): acceleration at every element node,
+  // 3*pnp*ntet in m/s^2 ([tet][node][xyz]); empty for JOB = 1.
+  std::vector<double> g0;
+  // Radial density profile of a generated ball, rho = rho_a + rho_b r / R.
+  bool has_profile = false;
+  double prof_a = 0.0, prof_b = 0.0, prof_R = 1.0;
   int n = 0, np = 0;
   bool fsexist = false, purefluid = false, assembled = false;
   int n_cout4 = 0;
@@ -803,6 +812,10 @@ int nmm_ball_create(const nmm_ball_opts* o, nmm_model** out) {
     }
   }
   const int pnp = m->pnp;
+  m->has_profile = true;
+  m->prof_R = o->radius;
+  m->prof_a = o->homogeneous ? o->rho0 : 13.0;
+  m->prof_b = o->homogeneous ? 0.0 : 3.3 - 13.0;
   m->vp.resize((size_t)pnp * m->ntet);
   m->vs.resize((size_t)pnp * m->ntet);
   m->rho.resize((size_t)pnp * m->ntet);
@@ -907,10 +920,135 @@ void elem_vertices(const nmm_model* m, int k, double v[4][3]) {
   }
 }
 
+// ---------------------------------------------------------------- gravity
+// Reference gravity (JOB = 2) quantities of one element
+// (src/mod_cg_create_matrix.f90:192-265 in CGFSE3D_ISO, :1057-1083 in
+// CGE3D_ISO): the nodal acceleration gk1 = g0 / 1e3 (km/s^2), its
+// least-squares gradient dgk1 over the element's nodes and, for the fluid
+// terms, the least-squares density gradient, N^2 and the unit vector along g.
+constexpr double kEps0 = 1.0e-15;  // eps0, src/mod_cg_create_matrix.f90:30
+
+struct GravElem {
+  std::vector<double> g;     // pnp x 3, km/s^2
+  double dg[3][3] = {};      // dg[a][c] = d g_c / d x_a
+  double drho[3] = {};       // d rho / d x_a
+  std::vector<double> n2;    // pnp: buoyancy frequency squared (fluid)
+  std::vector<double> unit;  // pnp x 3: g / max(|g|, eps0)
+};
+
+bool inv3(const double A[3][3], double X[3][3]) {
+  const double det = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) -
+                     A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
+                     A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+  if (!(det != 0.0) || !std::isfinite(det)) return false;
+  X[0][0] = (A[1][1] * A[2][2] - A[1][2] * A[2][1]) / det;
+  X[0][1] = (A[0][2] * A[2][1] - A[0][1] * A[2][2]) / det;
+  X[0][2] = (A[0][1] * A[1][2] - A[0][2] * A[1][1]) / det;
+  X[1][0] = (A[1][2] * A[2][0] - A[1][0] * A[2][2]) / det;
+  X[1][1] = (A[0][0] * A[2][2] - A[0][2] * A[2][0]) / det;
+  X[1][2] = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) / det;
+  X[2][0] = (A[1][0] * A[2][1] - A[1][1] * A[2][0]) / det;
+  X[2][1] = (A[0][1] * A[2][0] - A[0][0] * A[2][1]) / det;
+  X[2][2] = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) / det;
+  return true;
+}
+
+// lam: nodal lambda (kappa in a fluid); the N^2 fields are filled for fluid
+// elements only.  N^2 = (grad rho . g) / rho - |g|^2 rho / lambda, zero where
+// |g| < eps0 and everywhere in a pure-fluid planet (:233-255).
+bool grav_elem(const nmm_model* m, int k, const std::vector<double>& lam, bool fluid, GravElem& ge) {
+  const int p = m->pnp;
+  ge.g.assign(3 * (size_t)p, 0.0);
+  double xm[3] = {0, 0, 0}, gm[3] = {0, 0, 0}, rm = 0.0;
+  std::vector<double> X(3 * (size_t)p);
+  for (int l = 0; l < p; ++l) {
+    const double* x = &m->xyz[3 * (size_t)m->tet[(size_t)p * k + l]];
+    const double* g = &m->g0[3 * ((size_t)p * k + l)];
+    for (int c = 0; c < 3; ++c) {
+      X[3 * l + c] = x[c];
+      ge.g[3 * l + c] = g[c] / 1.0e3;
+      xm[c] += x[c];
+      gm[c] += ge.g[3 * l + c];
+    }
+    rm += m->rho[(size_t)p * k + l];
+  }
+  for (int c = 0; c < 3; ++c) {
+    xm[c] /= p;
+    gm[c] /= p;
+  }
+  rm /= p;
+  // dism = X - mean(X); dgk1 = (dism' dism)^-1 dism' (g - mean g)
+  double N[3][3] = {}, Ni[3][3], Rg[3][3] = {}, Rr[3] = {};
+  for (int l = 0; l < p; ++l) {
+    double d[3];
+    for (int c = 0; c < 3; ++c) d[c] = X[3 * l + c] - xm[c];
+    const double rd = m->rho[(size_t)p * k + l] - rm;
+    for (int a = 0; a < 3; ++a) {
+      for (int b = 0; b < 3; ++b) {
+        N[a][b] += d[a] * d[b];
+        Rg[a][b] += d[a] * (ge.g[3 * l + b] - gm[b]);
+      }
+      Rr[a] += d[a] * rd;
+    }
+  }
+  if (!inv3(N, Ni)) return false;
+  for (int a = 0; a < 3; ++a) {
+    ge.drho[a] = 0.0;
+    for (int c = 0; c < 3; ++c) {
+      ge.dg[a][c] = 0.0;
+      for (int b = 0; b < 3; ++b) ge.dg[a][c] += Ni[a][b] * Rg[b][c];
+    }
+    for (int b = 0; b < 3; ++b) ge.drho[a] += Ni[a][b] * Rr[b];
+  }
+  if (fluid) {
+    ge.n2.assign(p, 0.0);
+    ge.unit.assign(3 * (size_t)p, 0.0);
+    for (int l = 0; l < p; ++l) {
+      const double* g = &ge.g[3 * l];
+      const double rho = m->rho[(size_t)p * k + l];
+      const double ng = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+      double n2 = (ge.drho[0] * g[0] + ge.drho[1] * g[1] + ge.drho[2] * g[2]) / rho - ng * ng / lam[l] * rho;
+      if (ng < kEps0 || m->purefluid) n2 = 0.0;
+      ge.n2[l] = n2;
+      for (int c = 0; c < 3; ++c) ge.unit[3 * l + c] = g[c] / std::max(ng, kEps0);
+    }
+  }
+  return true;
+}
+
+// Gravity block (i, j) of a solid element, before the detJ factor
+// (src/mod_cg_create_matrix.f90:329-377, :1118-1160), G_j = diag(g_j):
+//   X = (D_i' M G_j + G_i M D_j) / 2 - M (dg_ij + dg_ji) / 2
+//       - (D_j' G_i M + M G_j D_i) / 2,   OPrho = (X R + R X) / 2, R = diag(rho).
+Mat solid_gravity_block(const RefElem& R, const Mat* D, const GravElem& ge, const std::vector<double>& rhot, int i,
+                        int j) {
+  const int p = R.pnp;
+  const Mat& M = R.M;
+  const double s = (ge.dg[i][j] + ge.dg[j][i]) / 2.0;
+  Mat X(p * p);
+  for (int a = 0; a < p; ++a)
+    for (int b = 0; b < p; ++b) {
+      double t1 = 0.0, t2 = 0.0, t3 = 0.0, t4 = 0.0;
+      for (int c = 0; c < p; ++c) {
+        t1 += D[i][c * p + a] * M[c * p + b];                      // (D_i' M)(a, b)
+        t2 += M[a * p + c] * D[j][c * p + b];                      // (M D_j)(a, b)
+        t3 += D[j][c * p + a] * ge.g[3 * c + i] * M[c * p + b];    // (D_j' G_i M)(a, b)
+        t4 += M[a * p + c] * ge.g[3 * c + j] * D[i][c * p + b];    // (M G_j D_i)(a, b)
+      }
+      t1 *= ge.g[3 * b + j];
+      t2 *= ge.g[3 * a + i];
+      X[a * p + b] = (t1 + t2) / 2.0 - M[a * p + b] * s - (t3 + t4) / 2.0;
+    }
+  Mat O(p * p);
+  for (int a = 0; a < p; ++a)
+    for (int b = 0; b < p; ++b) O[a * p + b] = (X[a * p + b] * rhot[b] + rhot[a] * X[a * p + b]) / 2.0;
+  return O;
+}
+
 // Solid element: TM (3pnp)^2 and MM (3pnp)^2.  `sym_mass` selects the
 // diag(rho)-symmetrised mass of CGE3D_ISO (src/mod_cg_create_matrix.f90:1089-1091)
 // instead of the mean-density mass of CGFSE3D_ISO (:293).
-void solid_element(const nmm_model* m, int k, const ElemGeom& g, bool sym_mass, double* TM, double* MM) {
+bool solid_element(const nmm_model* m, int k, const ElemGeom& g, bool sym_mass, double* TM, double* MM) {
   const int p = m->pnp, les = 3 * p;
   const RefElem& R = m->ref;
   std::vector<double> lam(p), mu(p), rhot(p);
@@ -959,6 +1097,9 @@ void solid_element(const nmm_model* m, int k, const ElemGeom& g, bool sym_mass, 
     for (int l = 0; l < p; ++l) srho += rhot[l];
     for (int a = 0; a < p * p; ++a) Mrho[a] = R.M[a] * srho / (double)p;
   }
+  GravElem ge;
+  const bool grav = !m->g0.empty();
+  if (grav && !grav_elem(m, k, lam, false, ge)) return false;
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
       Mat OPij(p * p);
@@ -976,30 +1117,49 @@ void solid_element(const nmm_model* m, int k, const ElemGeom& g, bool sym_mass, 
             OPtrsT[a * p + b] = b1[b * p + a] + b2[b * p + a];
         for (int a = 0; a < p * p; ++a) OPij[a] = (OPtrsT[a] + (a1[a] + a2[a])) / 2.0;
       }
+      if (grav) {
+        const Mat Og = solid_gravity_block(R, D, ge, rhot, i, j);
+        for (int a = 0; a < p * p; ++a) OPij[a] += Og[a];
+      }
       for (int a = 0; a < p; ++a)
         for (int b = 0; b < p; ++b) {
           TM[(size_t)(i * p + a) * les + (j * p + b)] = OPij[a * p + b] * g.detJ;
           MM[(size_t)(i * p + a) * les + (j * p + b)] = (i == j) ? Mrho[a * p + b] * g.detJ : 0.0;
         }
     }
+  return true;
 }
 
-// Fluid element, JOB = 1: FT and FM of dimension 3 pnp + pnp
-// (src/mod_cg_create_matrix.f90:453-640).  The face terms of :643-705 read
-// the reference gravity, which is zero without gravity, so they vanish.
-void fluid_element(const nmm_model* m, int k, const ElemGeom& g, double* FT, double* FM) {
+// Fluid element: FT and FM of dimension 3 pnp + pnp
+// (src/mod_cg_create_matrix.f90:453-640).  With the reference gravity
+// (JOB = 2) FT also carries
+//   * the N^2 displacement block (:492-608): (U_i M W_j + W_i M U_j) / 2 with
+//     U_i = diag(g_i / |g|), W_j = diag(g_j / |g| N^2 rho);
+//   * the density-gradient part of the coupling (:541-570): M D_i becomes
+//     M D_i - M diag(rho g_i / kappa);
+//   * the face terms of :643-705: on the outer boundary the pressure block
+//     gets -MassF sJac / (mean|g.n| mean rho) (free surface of a fluid); on an
+//     inner face that is not a fluid-solid face the displacement blocks get
+//     MassF sJac mean(g.n) mean(rho) n_j^2.
+// Without gravity the face terms vanish: they are built from the gravity
+// (zero in JOB = 1).  Returns NMM_OK or an error code.
+int fluid_element(const nmm_model* m, int k, const ElemGeom& g, double* FT, double* FM) {
   const int p = m->pnp, lef = 4 * p;
   const RefElem& R = m->ref;
-  std::vector<double> lamiv(p), rhot(p);
+  std::vector<double> lamiv(p), lam(p), rhot(p);
   double srho = 0.0;
   for (int l = 0; l < p; ++l) {
     size_t q = (size_t)p * k + l;
     double c44 = m->rho[q] * m->vs[q] * m->vs[q];
     double c33 = m->rho[q] * m->vp[q] * m->vp[q] - 2 * c44;
+    lam[l] = c33;
     lamiv[l] = 1.0 / std::sqrt(c33);
     rhot[l] = m->rho[q];
     srho += rhot[l];
   }
+  GravElem ge;
+  const bool grav = !m->g0.empty();
+  if (grav && !grav_elem(m, k, lam, true, ge)) return fail(NMM_ERR_MESH, "degenerate element in the gravity gradient");
   std::fill(FT, FT + (size_t)lef * lef, 0.0);
   std::fill(FM, FM + (size_t)lef * lef, 0.0);
   Mat flam(p * p), Mrho(p * p);
@@ -1015,6 +1175,9 @@ void fluid_element(const nmm_model* m, int k, const ElemGeom& g, double* FT, dou
     Mat Oij(p * p);
     for (int a = 0; a < p; ++a)
       for (int b = 0; b < p; ++b) Oij[a * p + b] = (G[a * p + b] + Ot[b * p + a]) / 2.0;
+    if (grav)
+      for (int a = 0; a < p; ++a)
+        for (int b = 0; b < p; ++b) Oij[a * p + b] -= R.M[a * p + b] * (rhot[b] / lam[b] * ge.g[3 * b + i]);
     for (int a = 0; a < p; ++a)
       for (int b = 0; b < p; ++b) {
         FM[(size_t)(i * p + a) * lef + (i * p + b)] = Mrho[a * p + b] * g.detJ;
@@ -1024,6 +1187,51 @@ void fluid_element(const nmm_model* m, int k, const ElemGeom& g, double* FT, dou
   }
   for (int a = 0; a < p; ++a)
     for (int b = 0; b < p; ++b) FT[(size_t)(3 * p + a) * lef + (3 * p + b)] = -(g.detJ * flam[a * p + b]);
+  if (!grav) return NMM_OK;
+  // N^2 block
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      for (int a = 0; a < p; ++a)
+        for (int b = 0; b < p; ++b) {
+          const double wj = ge.unit[3 * b + j] * ge.n2[b] * rhot[b];
+          const double wi = ge.unit[3 * a + i] * ge.n2[a] * rhot[a];
+          const double v = (ge.unit[3 * a + i] * R.M[a * p + b] * wj + wi * R.M[a * p + b] * ge.unit[3 * b + j]) / 2.0;
+          FT[(size_t)(i * p + a) * lef + (j * p + b)] = v * g.detJ;
+        }
+  // face terms
+  const int nfp = m->nfp;
+  for (int f = 0; f < 4; ++f) {
+    const std::vector<int>& Fm = R.fmask[f];
+    const std::vector<double>& MF = R.MF[f];
+    const double* nf = g.n[f];
+    double surfrho = 0.0, sgn = 0.0;
+    const bool outer = m->bface[4 * (size_t)k + f] != 0;
+    for (int a = 0; a < nfp; ++a) {
+      const double* gk = &ge.g[3 * Fm[a]];
+      const double gn = gk[0] * nf[0] + gk[1] * nf[1] + gk[2] * nf[2];
+      surfrho += rhot[Fm[a]];
+      sgn += outer ? std::sqrt(gn * gn) : gn;
+    }
+    surfrho /= nfp;
+    sgn /= nfp;
+    if (outer) {
+      if (!(sgn > 0.0)) return fail(NMM_ERR_MESH, "fluid boundary face without normal gravity");
+      for (int a = 0; a < nfp; ++a)
+        for (int b = 0; b < nfp; ++b)
+          FT[(size_t)(3 * p + Fm[a]) * lef + (3 * p + Fm[b])] -= MF[a * nfp + b] / sgn / surfrho * g.sJac[f];
+    } else {
+      int cout = 0;
+      for (int v = 0; v < 4; ++v)
+        if (v != f && m->rnum[m->tet[(size_t)p * k + R.vord[v]]] == 6) ++cout;
+      if (cout >= 3) continue;
+      for (int j = 0; j < 3; ++j)
+        for (int a = 0; a < nfp; ++a)
+          for (int b = 0; b < nfp; ++b)
+            FT[(size_t)(j * p + Fm[a]) * lef + (j * p + Fm[b])] +=
+                MF[a * nfp + b] * sgn * surfrho * g.sJac[f] * (nf[j] * nf[j]);
+    }
+  }
+  return NMM_OK;
 }
 
 // Sorted-neighbour lists (v2v, including the node itself).
@@ -1167,12 +1375,11 @@ extern "C" int nmm_element_matrices(const nmm_model* m, int k, double* T, double
   }
   if (!general || maxmu >= 1e-8) {
     *dim = 3 * m->pnp;
-    solid_element(m, k, g, !general, T, Mo);
-  } else {
-    *dim = 4 * m->pnp;
-    fluid_element(m, k, g, T, Mo);
+    if (!solid_element(m, k, g, !general, T, Mo)) return fail(NMM_ERR_MESH, "degenerate element in the gravity gradient");
+    return NMM_OK;
   }
-  return NMM_OK;
+  *dim = 4 * m->pnp;
+  return fluid_element(m, k, g, T, Mo);
 }
 
 extern "C" int nmm_assemble(nmm_model* m) {
@@ -1180,13 +1387,14 @@ extern "C" int nmm_assemble(nmm_model* m) {
   if (m->assembled) return NMM_OK;
   const bool general = m->fsexist || m->purefluid;
   const int p = m->pnp;
-  // Fluid element on the outer boundary: the JOB = 1 face term divides by the
-  // (zero) gravity there (src/mod_cg_create_matrix.f90:645-666).
-  for (int k = 0; k < m->ntet; ++k)
-    if (m->fluid[k])
-      for (int f = 0; f < 4; ++f)
-        if (m->bface[4 * (size_t)k + f])
-          return fail(NMM_ERR_MESH, "fluid element on the outer boundary is not supported without gravity");
+  // Fluid element on the outer boundary: the face term divides by the normal
+  // gravity there (src/mod_cg_create_matrix.f90:645-666), zero in JOB = 1.
+  if (m->g0.empty())
+    for (int k = 0; k < m->ntet; ++k)
+      if (m->fluid[k])
+        for (int f = 0; f < 4; ++f)
+          if (m->bface[4 * (size_t)k + f])
+            return fail(NMM_ERR_MESH, "fluid element on the outer boundary is not supported without gravity");
   auto adj = node_adjacency(m);
   if (general) {
     int rc = structure_general(m, adj);
@@ -1205,8 +1413,8 @@ extern "C" int nmm_assemble(nmm_model* m) {
   m->n_cout4 = 0;
   for (int k0 = 0; k0 < m->ntet; k0 += chunk) {
     int k1 = std::min(m->ntet, k0 + chunk);
-    int bad = 0;
-#pragma omp parallel for schedule(static) reduction(+ : bad)
+    int bad = 0, badg = 0, badf = 0;
+#pragma omp parallel for schedule(static) reduction(+ : bad, badg, badf)
     for (int k = k0; k < k1; ++k) {
       double v[4][3];
       elem_vertices(m, k, v);
@@ -1221,10 +1429,15 @@ extern "C" int nmm_assemble(nmm_model* m) {
       is_solid[k - k0] = solid;
       double* Tk = &T[(size_t)(k - k0) * lef * lef];
       double* Mk = &Mm[(size_t)(k - k0) * lef * lef];
-      if (solid) solid_element(m, k, g, !general, Tk, Mk);
-      else fluid_element(m, k, g, Tk, Mk);
+      if (solid) {
+        if (!solid_element(m, k, g, !general, Tk, Mk)) ++badg;
+      } else if (fluid_element(m, k, g, Tk, Mk) != NMM_OK) {
+        ++badf;
+      }
     }
     if (bad) return fail(NMM_ERR_MESH, "flat tetrahedron");
+    if (badg) return fail(NMM_ERR_MESH, "degenerate element in the gravity gradient");
+    if (badf) return fail(NMM_ERR_MESH, "fluid element: degenerate gravity gradient or boundary face without normal gravity");
     for (int k = k0; k < k1; ++k) {
       const int* nodes = &m->tet[(size_t)p * k];
       const double* Tk = &T[(size_t)(k - k0) * lef * lef];
@@ -1317,6 +1530,31 @@ extern "C" int nmm_assemble(nmm_model* m) {
               }
             }
           }
+          // Reference gravity on the interface (src/mod_cg_create_matrix.f90:866-920):
+          // the solid rows and columns of the face nodes lose
+          // rho_f sJac (n_p MF(a,b) g_q(b) + n_q g_p(a) MF(a,b)) / 2.
+          if (!m->g0.empty()) {
+            const double* nf = g.n[fcid];
+            double rhof = 0.0;
+            for (int a = 0; a < nfp; ++a) rhof += m->rho[(size_t)p * k + Fm[a]];
+            rhof /= nfp;
+            const double* gk = &m->g0[3 * (size_t)p * k];
+            for (int a = 0; a < nfp; ++a) {
+              const int na = nodes[Fm[a]];
+              for (int pp = 0; pp < 3; ++pp) {
+                const int row = m->vstt[na] + pp;
+                for (int b = 0; b < nfp; ++b) {
+                  const int pos = find_col(m->Ad, row, m->vstt[nodes[Fm[b]]]);
+                  if (pos < 0) return fail(NMM_ERR_STATE, "Ad interface structure miss");
+                  const double mf = MF[a * nfp + b];
+                  for (int q = 0; q < 3; ++q) {
+                    const double gq = gk[3 * Fm[b] + q] / 1.0e3, gp = gk[3 * Fm[a] + pp] / 1.0e3;
+                    m->Ad.val[pos + q] -= rhof * g.sJac[fcid] * (nf[pp] * mf * gq + nf[q] * gp * mf) / 2.0;
+                  }
+                }
+              }
+            }
+          }
         }
       }
     }
@@ -1399,6 +1637,57 @@ int nmm_set_material(nmm_model* m, const double* vp, const double* vs, const dou
   m->vs.assign(vs, vs + len);
   m->rho.assign(rho, rho + len);
   m->assembled = false;
+  return NMM_OK;
+}
+
+int nmm_set_gravity(nmm_model* m, const double* g0) {
+  if (!m) return fail(NMM_ERR_ARG, "null model");
+  const size_t len = 3 * (size_t)m->pnp * m->ntet;
+  if (g0) {
+    for (size_t i = 0; i < len; ++i)
+      if (!std::isfinite(g0[i])) return fail(NMM_ERR_ARG, "non-finite gravity value");
+    m->g0.assign(g0, g0 + len);
+  } else {
+    m->g0.clear();
+  }
+  m->assembled = false;
+  return NMM_OK;
+}
+
+int nmm_load_gravity(nmm_model* m, const char* base) {
+  if (!m || !base) return fail(NMM_ERR_ARG, "null argument");
+  const std::string path = std::string(base) + "_pod_" + std::to_string(m->porder) + "_potential_acceleration_true.dat";
+  std::vector<double> buf(3 * (size_t)m->pnp * m->ntet);
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return fail(NMM_ERR_IO, "cannot open " + path);
+  const size_t got = std::fread(buf.data(), sizeof(double), buf.size(), f);
+  std::fclose(f);
+  if (got != buf.size()) return fail(NMM_ERR_IO, "short gravity file " + path);
+  return nmm_set_gravity(m, buf.data());
+}
+
+// g(r) = G M(r) / r^2 with M(r) = 4 pi (a r^3 / 3 + b r^4 / (4 R)) for
+// rho = a + b r / R; r in km, rho in g/cm^3, so M in 1e12 kg and g in m/s^2
+// is G 4 pi 1e6 (a r / 3 + b r^2 / (4 R)).
+int nmm_ball_gravity(nmm_model* m, double G) {
+  if (!m) return fail(NMM_ERR_ARG, "null model");
+  if (!m->has_profile) return fail(NMM_ERR_STATE, "model has no radial density profile (load a gravity file instead)");
+  if (!(G > 0.0)) return fail(NMM_ERR_ARG, "G must be positive");
+  const int p = m->pnp;
+  std::vector<double> g0(3 * (size_t)p * m->ntet);
+  for (int k = 0; k < m->ntet; ++k)
+    for (int l = 0; l < p; ++l) {
+      const double* x = &m->xyz[3 * (size_t)m->tet[(size_t)p * k + l]];
+      const double r = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+      const double gr = G * 4.0 * M_PI * 1.0e6 * (m->prof_a * r / 3.0 + m->prof_b * r * r / (4.0 * m->prof_R));
+      for (int c = 0; c < 3; ++c) g0[3 * ((size_t)p * k + l) + c] = r > 0.0 ? -gr * x[c] / r : 0.0;
+    }
+  return nmm_set_gravity(m, g0.data());
+}
+
+int nmm_get_gravity(const nmm_model* m, const double** g0) {
+  if (!m || !g0) return fail(NMM_ERR_ARG, "null argument");
+  *g0 = m->g0.empty() ? nullptr : m->g0.data();
   return NMM_OK;
 }
 

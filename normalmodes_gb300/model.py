@@ -17,6 +17,11 @@ from . import build as _build
 
 _MATS = {"A": 0, "B": 1, "Ad": 2, "Ap": 3, "E": 4, "ET": 5}
 
+# Gravitational constant (m^3 kg^-1 s^-2) with which the reference's demo
+# gravity files are computed: |g| = 4/3 pi G rho r on the homogeneous CONST3k
+# model holds with this value to 1e-9.
+G_DEMO = 6.6723e-11
+
 
 class BallOpts(C.Structure):
     _fields_ = [
@@ -72,6 +77,10 @@ def lib() -> C.CDLL:
         L.nmm_write_results.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double,
                                         C.c_int, C.POINTER(C.c_double), C.c_longlong, C.c_char_p, C.c_int]
         L.nmm_set_material.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.nmm_set_gravity.argtypes = [vp, C.POINTER(C.c_double)]
+        L.nmm_load_gravity.argtypes = [vp, C.c_char_p]
+        L.nmm_ball_gravity.argtypes = [vp, C.c_double]
+        L.nmm_get_gravity.argtypes = [vp, C.POINTER(C.POINTER(C.c_double))]
         L.nmm_write_vector.argtypes = [C.c_char_p, C.POINTER(C.c_double), C.c_longlong]
         L.nmm_last_error.restype = C.c_char_p
         L.nmm_destroy.argtypes = [vp]
@@ -111,23 +120,59 @@ class Model:
         self._h = C.c_void_p(handle)
 
     @classmethod
-    def ball(cls, n_cells: int = 12, porder: int = 1, assemble: bool = True, **kw) -> "Model":
+    def ball(cls, n_cells: int = 12, porder: int = 1, assemble: bool = True, gravity: bool = False,
+             **kw) -> "Model":
+        """Layered ball; ``gravity=True`` adds the reference gravity of its
+        radial density profile (JOB = 2)."""
         o = default_opts(n_cells=n_cells, porder=porder, **kw)
         h = C.c_void_p()
         _check(lib().nmm_ball_create(C.byref(o), C.byref(h)))
         m = cls(h.value)
+        if gravity:
+            m.ball_gravity(assemble=False)
         if assemble:
             m.assemble()
         return m
 
     @classmethod
-    def load(cls, base_path: str, porder: int = 1, assemble: bool = True) -> "Model":
+    def load(cls, base_path: str, porder: int = 1, assemble: bool = True, gravity: bool = False) -> "Model":
+        """Model in the reference's input files; ``gravity=True`` also reads
+        ``<base>_pod_<p>_potential_acceleration_true.dat`` (JOB = 2)."""
         h = C.c_void_p()
         _check(lib().nmm_load_files(base_path.encode(), porder, C.byref(h)))
         m = cls(h.value)
+        if gravity:
+            _check(lib().nmm_load_gravity(m._h, base_path.encode()))
         if assemble:
             m.assemble()
         return m
+
+    def set_gravity(self, g0, assemble: bool = True) -> None:
+        """Reference gravity (ntet x pnp x 3, m/s^2) or None for JOB = 1."""
+        if g0 is None:
+            _check(lib().nmm_set_gravity(self._h, None))
+        else:
+            i = self.info()
+            a = np.ascontiguousarray(g0, dtype=np.float64).ravel()
+            if a.size != 3 * i.pnp * i.ntet:
+                raise ValueError(f"gravity needs {3 * i.pnp * i.ntet} values, got {a.size}")
+            _check(lib().nmm_set_gravity(self._h, a.ctypes.data_as(C.POINTER(C.c_double))))
+        if assemble:
+            self.assemble()
+
+    def ball_gravity(self, G: float = G_DEMO, assemble: bool = True) -> None:
+        _check(lib().nmm_ball_gravity(self._h, G))
+        if assemble:
+            self.assemble()
+
+    def gravity(self):
+        """The reference gravity (ntet x pnp x 3, m/s^2), or None (JOB = 1)."""
+        ptr = C.POINTER(C.c_double)()
+        _check(lib().nmm_get_gravity(self._h, C.byref(ptr)))
+        if not ptr:
+            return None
+        i = self.info()
+        return np.ctypeslib.as_array(ptr, shape=(3 * i.pnp * i.ntet,)).copy().reshape(i.ntet, i.pnp, 3)
 
     def assemble(self) -> None:
         _check(lib().nmm_assemble(self._h))
