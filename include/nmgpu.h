@@ -163,6 +163,45 @@ typedef struct {
 int nm_solve_batched(nm_ctx* ctx, const nm_slice* slices, int nslices, const nm_solve_opts* opts,
                      nm_result* results);
 
+/* Spectrum slicing by a kernel-polynomial (KPM) estimate of the eigenvalue
+ * density of B^-1 A.  No counterpart in the reference (one interval per
+ * job); the method is pEVSL's kpmdos + spslicer (Lin, Saad & Yang, SIAM
+ * Review 58, 2016), on the lambda-weighted density so that the zero modes of
+ * a fluid-solid pencil do not leak into the count:
+ *   mu_k = tr(T_k(S) B^-1 A) / n,  S = (B^-1 A - c) / e,  c, e the centre and
+ *   half-width of [lmin, lmax],
+ * estimated with nvec Rademacher vectors.  The count of (a, b] is the
+ * integral of the Jackson-damped expansion divided by lambda. */
+typedef int (*nm_block_op)(void* data, const double* X, double* Y, int ncols, int ld); /* Y = B^-1 A X */
+typedef struct {
+  int degree;              /* 0: nm_kpm_degree for the interval and slice count       */
+  int nvec;                /* random vectors (0: 16)                                  */
+  unsigned long long seed;
+  double ab_bounds[2];     /* bounds of B^-1 A; ab_bounds[1] <= 0: Lanczos bounds as in nm_solve */
+} nm_kpm_opts;
+void nm_default_kpm_opts(nm_kpm_opts* o);
+/* Degree whose Jackson kernel (about pi / d wide in theta = acos(t),
+ * t = (lambda - c) / e) is a quarter of the mean slice width in theta:
+ * 4 pi nslices / (theta(lam_lo) - theta(lam_hi)), clamped to [50, 4000];
+ * 0 for bad arguments. */
+int nm_kpm_degree(double lmin, double lmax, double lam_lo, double lam_hi, int nslices);
+/* Moments mu[0..degree] through a block operator (host arrays, n x ncols,
+ * leading dimension ld); runs on the host, so any operator will do. */
+int nm_kpm_moments(nm_block_op op, void* data, int n, double lmin, double lmax, int degree, int nvec,
+                   unsigned long long seed, double* mu);
+/* Estimated number of eigenvalues in (lam_lo, lam_hi], lam_lo > 0. */
+int nm_kpm_count(const double* mu, int degree, int n, double lmin, double lmax, double lam_lo, double lam_hi,
+                 double* count);
+/* nslices slices of [f_lo_mhz, f_hi_mhz] (f_lo_mhz > 0) with equal estimated
+ * counts; counts (nullable) receives the estimate per slice.  Frequencies
+ * map to eigenvalues as in nm_solve (src/mod_pevsl.f90:93-99). */
+int nm_kpm_slices(const double* mu, int degree, int n, double lmin, double lmax, double f_lo_mhz, double f_hi_mhz,
+                  int nslices, nm_slice* out, double* counts);
+/* All of the above on a context: Lanczos bounds (unless given), moments
+ * through nm_amv_block + nm_bsolve_block, slices for nm_solve_batched. */
+int nm_slice_spectrum(nm_ctx* ctx, double f_lo_mhz, double f_hi_mhz, int nslices, const nm_kpm_opts* opts,
+                      nm_slice* out, double* counts);
+
 /* Adjoint sensitivities.  No counterpart in the reference (it has no
  * gradients); the element model is the mesh, DOF map and nodal material of
  * the assembly behind the context's operators (nmm_mesh_arrays and

@@ -75,6 +75,13 @@ class NmSlice(C.Structure):
     _fields_ = [("f_lo_mhz", C.c_double), ("f_hi_mhz", C.c_double)]
 
 
+class NmKpmOpts(C.Structure):
+    _fields_ = [("degree", C.c_int), ("nvec", C.c_int), ("seed", C.c_ulonglong), ("ab_bounds", C.c_double * 2)]
+
+
+# int (*)(void* data, const double* X, double* Y, int ncols, int ld)
+NM_BLOCK_OP = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int, C.c_int)
+
 NM_ADJ_PAIR = 0
 NM_ADJ_MULTIPLET = 1
 
@@ -139,6 +146,15 @@ def lib() -> C.CDLL:
                                    C.POINTER(C.c_int), C.POINTER(C.c_longlong)]
         L.nm_test_sell.restype = C.c_longlong
         L.nm_test_start_vector.argtypes = [C.c_int, dp]
+        L.nm_default_kpm_opts.argtypes = [C.POINTER(NmKpmOpts)]
+        L.nm_kpm_degree.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
+        L.nm_kpm_moments.argtypes = [NM_BLOCK_OP, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
+                                     C.c_ulonglong, dp]
+        L.nm_kpm_count.argtypes = [dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, dp]
+        L.nm_kpm_slices.argtypes = [dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                    C.POINTER(NmSlice), dp]
+        L.nm_slice_spectrum.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.POINTER(NmKpmOpts),
+                                        C.POINTER(NmSlice), dp]
         _lib = L
     return _lib
 
@@ -321,6 +337,20 @@ class Solver:
             for i in range(len(slices)):
                 L.nm_result_free(C.byref(res[i]))
 
+    def slice_spectrum(self, lowfreq: float, upfreq: float, nslices: int, degree: int = 0, nvec: int = 16,
+                       seed: int = 0x4B504D, ab_bounds=None):
+        """nm_slice_spectrum: nslices [(f_lo, f_hi), ...] mHz slices of the
+        interval with equal estimated eigenvalue counts, and the estimates."""
+        o = NmKpmOpts()
+        lib().nm_default_kpm_opts(C.byref(o))
+        o.degree, o.nvec, o.seed = degree, nvec, seed
+        if ab_bounds is not None:
+            o.ab_bounds[0], o.ab_bounds[1] = ab_bounds
+        out = (NmSlice * nslices)()
+        counts = np.zeros(nslices)
+        self._check(lib().nm_slice_spectrum(self._h, lowfreq, upfreq, nslices, C.byref(o), out, _dp(counts)))
+        return [(out[i].f_lo_mhz, out[i].f_hi_mhz) for i in range(nslices)], counts
+
     def adjoint(self, mesh: dict, ref: dict, lam, X, mode: int = NM_ADJ_PAIR, tol: float = 1e-6):
         """Per-element sensitivities (rho, kappa, mu) of the eigenvalues `lam`
         with unscaled, B-normalised eigenvectors X (n x k), through
@@ -395,3 +425,54 @@ def start_vector(n: int) -> np.ndarray:
     out = np.zeros(n)
     lib().nm_test_start_vector(n, _dp(out))
     return out
+
+
+# ---------------------------------------------------------------- KPM slicing
+def kpm_degree(lmin: float, lmax: float, lam_lo: float, lam_hi: float, nslices: int) -> int:
+    return lib().nm_kpm_degree(lmin, lmax, lam_lo, lam_hi, nslices)
+
+
+def kpm_moments(apply, n: int, lmin: float, lmax: float, degree: int, nvec: int = 16,
+                seed: int = 0x4B504D) -> np.ndarray:
+    """nm_kpm_moments through a Python block operator: apply(X) returns
+    B^-1 A X for an n x ncols array."""
+    err = []
+
+    def cb(data, X, Y, ncols, ld):
+        try:
+            x = np.ctypeslib.as_array(X, shape=(ncols * ld,)).reshape(ncols, ld).T[:n]
+            y = np.ctypeslib.as_array(Y, shape=(ncols * ld,)).reshape(ncols, ld).T
+            y[:n] = apply(np.array(x))
+            return 0
+        except Exception as e:  # reported after the call
+            err.append(e)
+            return -1
+
+    f = NM_BLOCK_OP(cb)
+    mu = np.zeros(degree + 1)
+    rc = lib().nm_kpm_moments(f, None, n, lmin, lmax, degree, nvec, seed, _dp(mu))
+    if err:
+        raise err[0]
+    if rc != 0:
+        raise NmError(rc, "nm_kpm_moments failed")
+    return mu
+
+
+def kpm_count(mu, n: int, lmin: float, lmax: float, lam_lo: float, lam_hi: float) -> float:
+    mu = np.ascontiguousarray(mu, dtype=np.float64)
+    out = np.zeros(1)
+    rc = lib().nm_kpm_count(_dp(mu), len(mu) - 1, n, lmin, lmax, lam_lo, lam_hi, _dp(out))
+    if rc != 0:
+        raise NmError(rc, "nm_kpm_count: bad arguments")
+    return float(out[0])
+
+
+def kpm_slices(mu, n: int, lmin: float, lmax: float, lowfreq: float, upfreq: float, nslices: int):
+    mu = np.ascontiguousarray(mu, dtype=np.float64)
+    out = (NmSlice * nslices)()
+    counts = np.zeros(nslices)
+    rc = lib().nm_kpm_slices(_dp(mu), len(mu) - 1, n, lmin, lmax, lowfreq, upfreq, nslices, out, _dp(counts))
+    if rc != 0:
+        raise NmError(rc, "nm_kpm_slices: bad arguments")
+    return [(out[i].f_lo_mhz, out[i].f_hi_mhz) for i in range(nslices)], counts
+
