@@ -47,6 +47,16 @@ module nmgpu_mod
     real(c_double) :: t_filter, t_orth, t_eig
   end type nm_result
 
+  type, bind(C) :: nm_slice
+    real(c_double) :: f_lo_mhz, f_hi_mhz
+  end type nm_slice
+
+  type, bind(C) :: nm_kpm_opts
+    integer(c_int) :: degree, nvec
+    integer(c_long_long) :: seed          ! unsigned long long in C
+    real(c_double) :: ab_bounds(2)
+  end type nm_kpm_opts
+
   interface
     integer(c_int) function nm_create(ctx, A, B, Ap, E, ET, opts) bind(C, name="nm_create")
       import :: c_int, c_ptr, nm_csr, nm_opts
@@ -103,6 +113,34 @@ module nmgpu_mod
       type(nm_solve_opts), intent(in) :: opts
       type(nm_result), intent(inout) :: res
     end function nm_solve
+
+    ! several intervals on one context (no counterpart in the reference)
+    integer(c_int) function nm_solve_batched(ctx, slices, nslices, opts, results) &
+        bind(C, name="nm_solve_batched")
+      import :: c_int, c_ptr, nm_slice, nm_solve_opts, nm_result
+      type(c_ptr), value :: ctx
+      type(nm_slice), intent(in) :: slices(*)
+      integer(c_int), value :: nslices
+      type(nm_solve_opts), intent(in) :: opts
+      type(nm_result), intent(inout) :: results(*)
+    end function nm_solve_batched
+
+    subroutine nm_default_kpm_opts(o) bind(C, name="nm_default_kpm_opts")
+      import :: nm_kpm_opts
+      type(nm_kpm_opts), intent(out) :: o
+    end subroutine nm_default_kpm_opts
+
+    ! equal-count slices of [f_lo, f_hi] for nm_solve_batched (KPM estimate)
+    integer(c_int) function nm_slice_spectrum(ctx, f_lo_mhz, f_hi_mhz, nslices, opts, slices, counts) &
+        bind(C, name="nm_slice_spectrum")
+      import :: c_int, c_ptr, c_double, nm_kpm_opts, nm_slice
+      type(c_ptr), value :: ctx
+      real(c_double), value :: f_lo_mhz, f_hi_mhz
+      integer(c_int), value :: nslices
+      type(nm_kpm_opts), intent(in) :: opts
+      type(nm_slice), intent(out) :: slices(*)
+      real(c_double), intent(out) :: counts(*)
+    end function nm_slice_spectrum
 
     subroutine nm_result_free(res) bind(C, name="nm_result_free")
       import :: nm_result
