@@ -206,7 +206,9 @@ int nm_slice_spectrum(nm_ctx* ctx, double f_lo_mhz, double f_hi_mhz, int nslices
  * gradients); the element model is the mesh, DOF map and nodal material of
  * the assembly behind the context's operators (nmm_mesh_arrays and
  * nmm_reference return exactly these arrays).  All host arrays, borrowed for
- * the call. */
+ * the call.  The derivatives are those of the JOB = 1 element matrices: for
+ * operators assembled with the reference gravity (JOB = 2) the rho and kappa
+ * derivatives lack the gravity terms. */
 typedef struct {
   int ntet, pnp, nnode;
   int fluid_solid;                  /* 1: fluid-solid (general) model              */
