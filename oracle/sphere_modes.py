@@ -66,28 +66,30 @@ def _toroidal_f(omega, l, a, beta):
     return (l - 1) * _j(l, x) - x * _j(l + 1, x)
 
 
-def _roots(f, wmax, n=4000):
-    w = np.linspace(1e-6 * wmax, wmax, n)
-    v = np.array([f(x) for x in w])
+def _roots(f, wmax, wmin, n=4000):
+    """Sign changes of f on (wmin, wmax], refined by Brent's method.  f takes
+    arrays.  Below wmin (k a < 1e-2) the determinants vanish like a power of
+    omega and their sign is rounding noise, so no root is sought there."""
+    w = np.linspace(wmin, wmax, n)
+    with np.errstate(all="ignore"):
+        v = f(w)
     out = []
-    for i in range(n - 1):
-        if np.isfinite(v[i]) and np.isfinite(v[i + 1]) and v[i] * v[i + 1] < 0:
-            out.append(brentq(f, w[i], w[i + 1], xtol=1e-14, rtol=1e-14))
+    for i in np.flatnonzero(np.isfinite(v[:-1]) & np.isfinite(v[1:]) & (v[:-1] * v[1:] < 0)):
+        out.append(brentq(lambda x: float(f(np.array([x]))[0]), w[i], w[i + 1], xtol=1e-14, rtol=1e-14))
     return out
 
 
 def mode_table(fmax_mhz: float, a=6371.0, alpha=10.0, beta=5.7735, rho=5.51, lmax=30):
     """List of (freq_mHz, kind 'S'|'T', n, l, multiplicity 2l+1) below fmax."""
     wmax = 2 * math.pi * fmax_mhz * 1e-3
+    wmin = 1e-2 * beta / a
     modes = []
     for l in range(0, lmax + 1):
-        ws = _roots(lambda w: _spheroidal_det(w, l, a, alpha, beta, rho), wmax)
-        if l == 1:
-            ws = [w for w in ws if w > 1e-9]
+        ws = _roots(lambda w: _spheroidal_det(w, l, a, alpha, beta, rho), wmax, wmin)
         for n_, w in enumerate(ws):
             modes.append((w / (2 * math.pi) * 1e3, "S", n_, l, 2 * l + 1))
         if l >= 1:
-            wt = _roots(lambda w: _toroidal_f(w, l, a, beta), wmax)
+            wt = _roots(lambda w: _toroidal_f(w, l, a, beta), wmax, wmin)
             for n_, w in enumerate(wt):
                 modes.append((w / (2 * math.pi) * 1e3, "T", n_, l, 2 * l + 1))
     modes.sort()

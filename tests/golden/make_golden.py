@@ -28,6 +28,10 @@ SPECS = {
     "solid_p1": dict(model=dict(n_cells=6, porder=1, fluid_core=0), porder=1, interval=(0.2, 1.0), dense=True),
     "fs_p1": dict(model=dict(n_cells=8, porder=1), porder=1, interval=(0.2, 1.0), dense=True),
     "fs_p2": dict(model=dict(n_cells=8, porder=2), porder=2, interval=(0.2, 0.6), dense=False),
+    # reference gravity (JOB = 2) of the balls' own density profile
+    "solid_p1_grav": dict(model=dict(n_cells=6, porder=1, fluid_core=0, gravity=True), porder=1,
+                          interval=(0.1, 1.0), dense=True),
+    "fs_p1_grav": dict(model=dict(n_cells=8, porder=1, gravity=True), porder=1, interval=(0.2, 1.0), dense=True),
 }
 
 

@@ -1,0 +1,64 @@
+"""CPU tests that pin the oracle: the golden fixtures against dense LAPACK
+solves of the same pencils, the oracle reproducing its fixtures, and the
+assembled operators of a homogeneous ball against the analytic spectrum of a
+homogeneous elastic sphere (Lamb 1882)."""
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _golden(name):
+    return np.load(os.path.join(HERE, "golden", f"{name}.npz"))
+
+
+@pytest.mark.parametrize("name", ["solid_p1", "fs_p1", "solid_p1_grav", "fs_p1_grav"])
+def test_golden_fixtures_match_dense_solves(name):
+    """The oracle's filtered-Lanczos eigenvalues (the fixtures the GPU tests
+    compare with) against scipy.linalg.eigh of the same pencil."""
+    g = _golden(name)
+    assert len(g["lam"]) == len(g["lam_dense"]) > 0
+    assert np.max(np.abs(g["lam"] - g["lam_dense"]) / g["lam_dense"]) < 1e-10
+    assert np.max(g["err_ref"]) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["solid_p1", "solid_p1_grav"])
+def test_oracle_reproduces_its_fixture(name):
+    import ast
+
+    from normalmodes_gb300.model import Model
+    from oracle import oracle as O
+    g = _golden(name)
+    m = Model.ball(**ast.literal_eval(str(g["model_kw"])))
+    op = O.setup_operator(m.operators(), int(g["porder"]), bounds={"B": tuple(g["b_bounds"])})
+    lo, hi = (float(x) for x in g["interval"])
+    r = O.apply_pevsl(op, lo, hi, ab_bounds=(float(g["xintv"][2]), float(g["xintv"][3])))
+    assert r.pol.deg == int(g["pol_deg"])
+    assert len(r.lam) == len(g["lam"])
+    assert np.max(np.abs(r.lam - g["lam"]) / g["lam"]) < 1e-12
+
+
+def test_homogeneous_ball_matches_the_analytic_sphere():
+    """P2 homogeneous solid ball (vp 10, vs 5.7735 km/s, rho 5.51 g/cm^3):
+    six rigid modes at zero, then the lowest 34 singlets within 2 % (6 cells
+    per axis) and 1 % (8 cells) of the analytic frequencies, the error
+    shrinking with the mesh."""
+    from scipy.sparse.linalg import eigsh
+
+    from normalmodes_gb300.model import Model
+    from oracle import sphere_modes as S
+    fa = S.singlet_frequencies(1.0)
+    assert fa[0] == pytest.approx(0.3607351, rel=1e-6)  # 0T2
+    mean = {}
+    for nc, tol in ((6, 0.02), (8, 0.01)):
+        m = Model.ball(n_cells=nc, porder=2, fluid_core=0, homogeneous=1, jitter=0.0)
+        A, B = m.csr("A").to_scipy().tocsc(), m.csr("B").to_scipy().tocsc()
+        w = np.sort(eigsh(A, k=40, M=B, sigma=2e-6, which="LM", return_eigenvectors=False))
+        f = np.sqrt(np.maximum(w, 0.0)) / (2 * np.pi) * 1e3
+        assert f[:6].max() < 1e-6
+        rel = np.abs(f[6:40] - fa[:34]) / fa[:34]
+        assert rel.max() < tol, (nc, rel.max())
+        mean[nc] = rel.mean()
+    assert mean[8] < 0.6 * mean[6]
