@@ -206,9 +206,9 @@ int nm_slice_spectrum(nm_ctx* ctx, double f_lo_mhz, double f_hi_mhz, int nslices
  * gradients); the element model is the mesh, DOF map and nodal material of
  * the assembly behind the context's operators (nmm_mesh_arrays and
  * nmm_reference return exactly these arrays).  All host arrays, borrowed for
- * the call.  The derivatives are those of the JOB = 1 element matrices: for
- * operators assembled with the reference gravity (JOB = 2) the rho and kappa
- * derivatives lack the gravity terms. */
+ * the call.  With g0 set (operators assembled with the reference gravity,
+ * JOB = 2) the gravity terms are differentiated too, the field held fixed
+ * (nm_adjoint_gravity). */
 typedef struct {
   int ntet, pnp, nnode;
   int fluid_solid;                  /* 1: fluid-solid (general) model              */
@@ -221,7 +221,19 @@ typedef struct {
   const double *vp, *vs, *rho;      /* pnp*ntet nodal material                      */
   const double* ref_mass;           /* pnp*pnp, row-major                           */
   const double* ref_drst;           /* 3*pnp*pnp, d/dr, d/ds, d/dt                  */
+  const double* g0;                 /* 3*pnp*ntet reference gravity (m/s^2) or NULL  */
+  const double* ref_massf;          /* 4*nfp*nfp face masses (needed with g0)        */
+  const int* ref_fmask;             /* 4*nfp face node lists, 0-based (with g0)      */
 } nm_elem_model;
+
+/* The reference-gravity terms of the sensitivities (JOB = 2,
+ * src/mod_cg_create_matrix.f90:192-265, 329-377, 492-705, 866-920): ADDS
+ * them to grad (k x ntet x 3, per pair) for unscaled eigenvectors X
+ * (n x k, leading dimension ldx) and their pressures P (np x k, ldp; NULL
+ * for a solid model).  Host code, no GPU; nm_adjoint calls it when em->g0
+ * is set. */
+int nm_adjoint_gravity(const nm_elem_model* em, int k, const double* X, int ldx, const double* P, int ldp,
+                       double* grad);
 
 #define NM_ADJ_PAIR 0      /* one gradient per eigenpair                          */
 #define NM_ADJ_MULTIPLET 1 /* one per group of eigenvalues within tol (relative) */

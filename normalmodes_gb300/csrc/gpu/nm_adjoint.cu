@@ -19,7 +19,8 @@
 // whose derivative for a uniform shift of lambda = kappa gives
 //   dlam/dkappa_e = detJ (p .* lambda^-3/2)^T M (p .* lambda^-1/2).
 // Each thread recomputes its element's geometry and nodal fields for one
-// eigenvector; nothing per element is stored.
+// eigenvector; nothing per element is stored.  With the reference gravity
+// (JOB = 2) the host adds the gravity terms (nm_adjoint_gravity).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -186,6 +187,8 @@ int nm_adjoint(nm_ctx* c, const nm_elem_model* em, int k, const double* lam, con
   if (!em->tets || !em->xyz || !em->fluid || !em->vstt || !em->rnum || !em->vp || !em->vs || !em->rho ||
       !em->ref_mass || !em->ref_drst || (c->fs && !em->pstt))
     return set_err(c, NM_ERR_ARG, "nm_adjoint: missing element-model array");
+  if (em->g0 && (!em->ref_massf || !em->ref_fmask))
+    return set_err(c, NM_ERR_ARG, "nm_adjoint: gravity terms need the reference face masses and face lists");
   // every DOF the elements address must exist
   for (int e = 0; e < ntet; ++e)
     for (int a = 0; a < P; ++a) {
@@ -247,7 +250,7 @@ int nm_adjoint(nm_ctx* c, const nm_elem_model* em, int k, const double* lam, con
     return rc;
   }
   // per-pair gradients (host)
-  std::vector<double> pair;
+  std::vector<double> pair, hP;
   double* out_pairs = grad;
   if (mode == NM_ADJ_MULTIPLET) {
     pair.resize((size_t)k * ntet * 3);
@@ -280,7 +283,16 @@ int nm_adjoint(nm_ctx* c, const nm_elem_model* em, int k, const double* lam, con
     NM_CUDA(c, cudaGetLastError());
     NM_CUDA(c, cudaMemcpyAsync(out_pairs + (size_t)j0 * ntet * 3, dg, sizeof(double) * (size_t)m * ntet * 3,
                                cudaMemcpyDeviceToHost, s));
+    if (em->g0 && c->fs) {
+      hP.resize((size_t)np * m);
+      NM_CUDA(c, cudaMemcpyAsync(hP.data(), dP, sizeof(double) * (size_t)np * m, cudaMemcpyDeviceToHost, s));
+    }
     NM_CUDA(c, cudaStreamSynchronize(s));
+    if (em->g0 && (rc = nm_adjoint_gravity(em, m, X + (size_t)j0 * ldx, ldx, c->fs ? hP.data() : nullptr, np,
+                                           out_pairs + (size_t)j0 * ntet * 3))) {
+      release();
+      return set_err(c, rc, "nm_adjoint: gravity terms failed (degenerate element)");
+    }
   }
   release();
   if ((rc = check_status(c))) return rc;

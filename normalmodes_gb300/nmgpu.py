@@ -68,7 +68,57 @@ class NmElemModel(C.Structure):
     _fields_ = [("ntet", C.c_int), ("pnp", C.c_int), ("nnode", C.c_int), ("fluid_solid", C.c_int),
                 ("tets", C.c_void_p), ("xyz", C.c_void_p), ("fluid", C.c_void_p), ("vstt", C.c_void_p),
                 ("rnum", C.c_void_p), ("pstt", C.c_void_p), ("vp", C.c_void_p), ("vs", C.c_void_p),
-                ("rho", C.c_void_p), ("ref_mass", C.c_void_p), ("ref_drst", C.c_void_p)]
+                ("rho", C.c_void_p), ("ref_mass", C.c_void_p), ("ref_drst", C.c_void_p), ("g0", C.c_void_p),
+                ("ref_massf", C.c_void_p), ("ref_fmask", C.c_void_p)]
+
+
+def _elem_model(mesh: dict, ref: dict, fluid_solid: bool, g0=None):
+    """nm_elem_model over contiguous copies of the arrays; returns the struct
+    and the copies (keep them alive for the call)."""
+    nt, pnp = mesh["tets"].shape
+    keep = {
+        "tets": np.ascontiguousarray(mesh["tets"], dtype=np.int32),
+        "xyz": np.ascontiguousarray(mesh["xyz"], dtype=np.float64),
+        "fluid": np.ascontiguousarray(mesh["fluid"], dtype=np.uint8),
+        "vstt": np.ascontiguousarray(mesh["vstt"], dtype=np.int32),
+        "rnum": np.ascontiguousarray(mesh["rnum"], dtype=np.int32),
+        "pstt": np.ascontiguousarray(mesh["pstt"], dtype=np.int32),
+        "vp": np.ascontiguousarray(mesh["vp"], dtype=np.float64),
+        "vs": np.ascontiguousarray(mesh["vs"], dtype=np.float64),
+        "rho": np.ascontiguousarray(mesh["rho"], dtype=np.float64),
+        "M": np.ascontiguousarray(ref["M"], dtype=np.float64),
+        "D": np.ascontiguousarray(ref["Drst"], dtype=np.float64),
+        "MF": np.ascontiguousarray(ref["MassF"], dtype=np.float64),
+        "FM": np.ascontiguousarray(ref["Fmask"], dtype=np.int32),
+    }
+    gp = None
+    if g0 is not None:
+        keep["g0"] = np.ascontiguousarray(g0, dtype=np.float64)
+        gp = keep["g0"].ctypes.data
+    em = NmElemModel(nt, pnp, mesh["xyz"].shape[0], int(fluid_solid),
+                     *[keep[q].ctypes.data for q in ("tets", "xyz", "fluid", "vstt", "rnum", "pstt", "vp", "vs",
+                                                     "rho", "M", "D")],
+                     gp, keep["MF"].ctypes.data, keep["FM"].ctypes.data)
+    return em, keep
+
+
+def adjoint_gravity(mesh: dict, ref: dict, g0, X, P=None, fluid_solid: bool = False) -> np.ndarray:
+    """nm_adjoint_gravity (host code, no GPU): the reference-gravity terms of
+    the per-pair sensitivities, (k, ntet, 3)."""
+    X = np.asfortranarray(X, dtype=np.float64)
+    if X.ndim == 1:
+        X = X[:, None]
+    k = X.shape[1]
+    em, keep = _elem_model(mesh, ref, fluid_solid, g0)
+    grad = np.zeros((k, mesh["tets"].shape[0], 3))
+    Pp, ldp = None, 0
+    if P is not None:
+        P = np.asfortranarray(P, dtype=np.float64).reshape(-1, k)
+        Pp, ldp = _dp(P), P.shape[0]
+    rc = lib().nm_adjoint_gravity(C.byref(em), k, _dp(X), X.shape[0], Pp, ldp, _dp(grad))
+    if rc != 0:
+        raise NmError(rc, "nm_adjoint_gravity failed")
+    return grad
 
 
 class NmSlice(C.Structure):
@@ -140,6 +190,7 @@ def lib() -> C.CDLL:
         L.nm_solve_batched.argtypes = [vp, C.POINTER(NmSlice), C.c_int, C.POINTER(NmSolveOpts), C.POINTER(NmResult)]
         L.nm_adjoint.argtypes = [vp, C.POINTER(NmElemModel), C.c_int, dp, dp, C.c_int, C.c_int, C.c_double, dp,
                                  C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.nm_adjoint_gravity.argtypes = [C.POINTER(NmElemModel), C.c_int, dp, C.c_int, dp, C.c_int, dp]
         L.nm_test_find_pol.argtypes = [dp, C.c_double, C.c_double, C.c_int, dp, C.c_int, dp]
         L.nm_test_tridiag.argtypes = [dp, dp, C.c_int, C.c_double, C.c_double, dp, dp, C.c_int]
         L.nm_test_sell.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), dp,
@@ -351,31 +402,17 @@ class Solver:
         self._check(lib().nm_slice_spectrum(self._h, lowfreq, upfreq, nslices, C.byref(o), out, _dp(counts)))
         return [(out[i].f_lo_mhz, out[i].f_hi_mhz) for i in range(nslices)], counts
 
-    def adjoint(self, mesh: dict, ref: dict, lam, X, mode: int = NM_ADJ_PAIR, tol: float = 1e-6):
+    def adjoint(self, mesh: dict, ref: dict, lam, X, mode: int = NM_ADJ_PAIR, tol: float = 1e-6, g0=None):
         """Per-element sensitivities (rho, kappa, mu) of the eigenvalues `lam`
         with unscaled, B-normalised eigenvectors X (n x k), through
-        nm_adjoint.  `mesh` is Model.mesh(), `ref` Model.reference().
+        nm_adjoint.  `mesh` is Model.mesh(), `ref` Model.reference(), `g0`
+        Model.gravity() for operators assembled with the reference gravity.
         Returns (grad[k or ngroups, ntet, 3], group[k])."""
         lam = np.ascontiguousarray(lam, dtype=np.float64)
         X = np.asfortranarray(X, dtype=np.float64)
         k = lam.size
-        nt, pnp = mesh["tets"].shape
-        keep = {
-            "tets": np.ascontiguousarray(mesh["tets"], dtype=np.int32),
-            "xyz": np.ascontiguousarray(mesh["xyz"], dtype=np.float64),
-            "fluid": np.ascontiguousarray(mesh["fluid"], dtype=np.uint8),
-            "vstt": np.ascontiguousarray(mesh["vstt"], dtype=np.int32),
-            "rnum": np.ascontiguousarray(mesh["rnum"], dtype=np.int32),
-            "pstt": np.ascontiguousarray(mesh["pstt"], dtype=np.int32),
-            "vp": np.ascontiguousarray(mesh["vp"], dtype=np.float64),
-            "vs": np.ascontiguousarray(mesh["vs"], dtype=np.float64),
-            "rho": np.ascontiguousarray(mesh["rho"], dtype=np.float64),
-            "M": np.ascontiguousarray(ref["M"], dtype=np.float64),
-            "D": np.ascontiguousarray(ref["Drst"], dtype=np.float64),
-        }
-        em = NmElemModel(nt, pnp, mesh["xyz"].shape[0], int(self.info().fs),
-                         *[keep[q].ctypes.data for q in ("tets", "xyz", "fluid", "vstt", "rnum", "pstt", "vp", "vs",
-                                                         "rho", "M", "D")])
+        nt = mesh["tets"].shape[0]
+        em, keep = _elem_model(mesh, ref, bool(self.info().fs), g0)
         grad = np.zeros((k, nt, 3))
         group = np.zeros(k, dtype=np.int32)
         ng = C.c_int()
