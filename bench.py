@@ -54,6 +54,11 @@ WORKLOADS = {
     "ball12-p1": dict(
         desc="layered ball, 10,368 P1 tets, 0.2-1.0 mHz",
         model=dict(n_cells=12, porder=1), porder=1, interval=(0.2, 1.0)),
+    "ball36-p2-lateral-grav": dict(
+        desc="layered ball, 279,936 P2 tets, 1.2M DOF, +-2% degree-8 lateral perturbation, reference gravity "
+             "(JOB = 2), 0.1-2.0 mHz",
+        model=dict(n_cells=36, porder=2, lateral_pert=0.02, lateral_lmax=8, gravity=True), porder=2,
+        interval=(0.1, 2.0)),
 }
 # Step counts of the reference algorithm (single-vector ChebLanNr, FP64) on
 # the 1.2M-DOF ball, measured on GB300; used only to project CPU samples.

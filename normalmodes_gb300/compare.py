@@ -1,7 +1,7 @@
 """Mixed precision against FP64 on one spectrum slice.
 
     python -m normalmodes_gb300.compare [--cells 24] [--porder 2] [--lateral 0.02]
-                                        [--interval 0.1 1.0] [--fp64-block 32|0]
+                                        [--interval 0.1 1.0] [--fp64-block 32|0] [--gravity]
 
 Solves the interval twice on one GPU: the mixed path (FP32 filter SpMMs,
 FP64 Lanczos and Rayleigh-Ritz, block of 32) and the FP64 path (block of 32,
@@ -29,15 +29,17 @@ def main(argv=None) -> None:
     ap.add_argument("--polish", type=int, default=0, help="mixed path refinement degree (0: default, <0: off)")
     ap.add_argument("--fp64-lam", default=None, help="eigenvalues of an earlier FP64 solve (.npy) instead of solving")
     ap.add_argument("--save-fp64-lam", default=None, help="write the FP64 eigenvalues to this .npy file")
+    ap.add_argument("--gravity", action="store_true", help="operators with the reference gravity (JOB = 2)")
     a = ap.parse_args(argv)
     from normalmodes_gb300.model import Model
     from normalmodes_gb300.nmgpu import NM_PREC_FP64, NM_PREC_MIXED, Solver
     kw = dict(n_cells=a.cells, porder=a.porder)
     if a.lateral > 0:
         kw.update(lateral_pert=a.lateral, lateral_lmax=8)
-    mats = Model.ball(**kw).operators()
+    mats = Model.ball(gravity=a.gravity, **kw).operators()
     lo, hi = a.interval
-    out = {"cells": a.cells, "porder": a.porder, "lateral": a.lateral, "interval_mhz": [lo, hi], "polish": a.polish}
+    out = {"cells": a.cells, "porder": a.porder, "lateral": a.lateral, "interval_mhz": [lo, hi], "polish": a.polish,
+           "gravity": a.gravity}
     res = {}
     runs = [("mixed", NM_PREC_MIXED, 32)] + ([] if a.fp64_lam else [("fp64", NM_PREC_FP64, a.fp64_block)])
     for name, prec, block in runs:
