@@ -1,0 +1,125 @@
+"""CPU tests of the job driver (python -m normalmodes_gb300.run): the
+reference's global_conf rules (src/mod_para.f90:79-137, src/mod_string.f90),
+dry runs over models in the reference's input files with and without the
+reference gravity, and a whole job whose GPU solve is replaced by the oracle
+(the printed tables and the result files)."""
+import io
+import os
+
+import numpy as np
+import pytest
+
+from normalmodes_gb300 import run as R
+
+REF_DEMO = os.environ.get("NM_REFERENCE_DEMOS", "/root/reference/demos/models/input")
+
+
+def _write_conf(path, **kv):
+    lines = ["# JOB: normal modes modelling", "# 1 without gravity, 2 with reference gravity"]
+    for k, v in kv.items():
+        lines.append(f"{k:<11} = {v}   # comment")
+    path.write_text("\n".join(lines) + "\n")
+    return str(path)
+
+
+def test_reference_demo_configurations():
+    demos = os.path.dirname(os.path.dirname(REF_DEMO))
+    conf = os.path.join(demos, "global_conf")
+    if not os.path.exists(conf):
+        pytest.skip("reference demos not present")
+    j = R.read_global_conf(conf)
+    assert (j.job, j.basename, j.inputdir, j.outputdir, j.porder) == (
+        1, "CONST_1L_3k.1", "models/input/CONST3k/", "models/output/CONST3k/", 1)
+    assert j.lowfreq == float(np.float32(0.2)) and j.upfreq == 2.0 and not j.gravity
+
+
+def test_configuration_rules(tmp_path):
+    p = tmp_path / "global_conf"
+    p.write_text("\n".join([
+        "# a comment line",
+        "JOB=2",
+        "JOB = 1          # the first line of a key wins",
+        "basename\tball.1",
+        "#basename = other",
+        "inputdir   = in/   # trailing comment",
+        "outputdir  = out/",
+        "lowfreq = 0.1 # mHz",
+        "upfreq  = 1.0",
+        "pOrder  = 2",
+    ]) + "\n")
+    j = R.read_global_conf(str(p))
+    assert (j.job, j.basename, j.inputdir, j.outputdir, j.porder) == (2, "ball.1", "in/", "out/", 2)
+    assert j.lowfreq == float(np.float32(0.1)) and j.gravity and j.base_path == "in/ball.1"
+    base = dict(JOB=1, basename="b", inputdir="i/", outputdir="o/", lowfreq=0.1, upfreq=1.0, pOrder=1)
+    for bad, msg in ((dict(lowfreq=1.0), "frequencies"), (dict(JOB=20), "not supported"),
+                     (dict(pOrder=3), "pOrder")):
+        with pytest.raises(R.ConfError, match=msg):
+            R.read_global_conf(_write_conf(tmp_path / "c", **{**base, **bad}))
+    kv = dict(base)
+    del kv["outputdir"]
+    with pytest.raises(R.ConfError, match="there is no outputdir"):
+        R.read_global_conf(_write_conf(tmp_path / "c", **kv))
+    with pytest.raises(R.ConfError, match="does not exist"):
+        R.read_global_conf(str(tmp_path / "missing"))
+    assert R.main([str(tmp_path / "missing")]) == 2
+
+
+def _job_files(tmp_path, job, porder=1, **ball):
+    from normalmodes_gb300.model import Model
+    from tests.test_gravity import _write_reference_files
+    src = Model.ball(n_cells=6, porder=porder, fluid_core=0, gravity=True, assemble=False, **ball)
+    inp = tmp_path / "input"
+    inp.mkdir(exist_ok=True)
+    base = _write_reference_files(src, str(inp), "ball.1", porder)
+    src.gravity().astype(np.float64).tofile(base + f"_pod_{porder}_potential_acceleration_true.dat")
+    return _write_conf(tmp_path / "global_conf", JOB=job, basename="ball.1", inputdir=str(inp) + "/",
+                       outputdir=str(tmp_path / "output") + "/", lowfreq=0.1, upfreq=1.0, pOrder=porder)
+
+
+@pytest.mark.parametrize("job", [1, 2])
+def test_dry_run(tmp_path, job):
+    conf = _job_files(tmp_path, job)
+    out = io.StringIO()
+    s = R.run(R.read_global_conf(conf), dry_run=True, out=out)
+    assert s["gravity"] == (job == 2) and s["n"] > 0 and s["ntet"] == 1296
+    assert "reference gravity" in out.getvalue() or job == 1
+
+
+class _OracleSolver:
+    """Stand-in for the GPU context: the oracle's solve, unscaled vectors."""
+
+    def __init__(self, mats, porder, mixed):
+        from oracle import oracle as O
+        self.O, self.op = O, O.setup_operator(mats, porder)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+    def solve(self, lo, hi, want_vectors, unscale, block):
+        r = self.O.apply_pevsl(self.op, lo, hi)
+        r.vec = r.Y * self.op.D[:, None] if unscale else r.Y
+        return r
+
+
+def test_whole_job_with_a_stand_in_solver(tmp_path, monkeypatch):
+    from oracle import oracle as O
+    conf = _job_files(tmp_path, 2)
+    monkeypatch.setattr(R, "make_solver", _OracleSolver)
+    out = io.StringIO()
+    s = R.run(R.read_global_conf(conf), out=out)
+    text = out.getvalue()
+    assert s["nev"] > 0
+    f, T = O.freq_mhz(s["lam"])
+    rows = [ln.split() for ln in text.splitlines() if ln.strip().startswith("Row") and "err." not in ln]
+    assert len(rows) == s["nev"]
+    assert np.allclose([float(r[2]) for r in rows], f, rtol=1e-12)
+    assert np.allclose([float(r[3]) for r in rows], T, rtol=1e-12)
+    prefix = s["prefix"]
+    assert os.path.basename(prefix).startswith("ball.1_JOB2_pod1_np1_")
+    vec1 = np.fromfile(prefix + "_1.dat")
+    assert vec1.size == s["n"]
+    assert os.path.exists(str(tmp_path / "output" / "ball.1_pod1_np1_vlist.dat"))
+    assert not os.path.exists(prefix + f"_{s['nev'] + 1}.dat")
