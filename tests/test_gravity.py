@@ -177,7 +177,8 @@ def test_bad_gravity_rejected(tmp_path):
 REF_DEMOS = os.environ.get("NM_REFERENCE_DEMOS", "/root/reference/demos/models/input")
 
 
-@pytest.mark.parametrize("model,porder", [("PREM3k/prem_3L_3k.1", 1), ("CONST3k/CONST_1L_3k.1", 2)])
+@pytest.mark.parametrize("model,porder", [("PREM3k/prem_3L_3k.1", 1), ("CONST3k/CONST_1L_3k.1", 2),
+                                          ("RTMDWAK8k/RTMDWAK_3L_8k.1", 1)])
 def test_reference_demo_models(model, porder):
     """The reference's demo models with their own gravity files: the C++
     assembly against the numpy restatement; the CONST3k field is
@@ -215,3 +216,19 @@ def test_filtered_lanczos_on_gravity_pencil():
     assert np.max(np.abs(r.lam - ref) / ref) < 1e-10
     f = O.freq_mhz(ref[:3])[0]
     assert np.ptp(f) < 1e-6 * f[0]  # three-fold degenerate
+
+
+@pytest.mark.parametrize("model", ["PREM3k/prem_3L_3k.1", "CONST3k/CONST_1L_3k.1", "RTMDWAK8k/RTMDWAK_3L_8k.1"])
+def test_boundary_faces_match_the_reference_neighbour_files(model):
+    """The outer-boundary faces the gravity face terms use, derived from the
+    tetrahedra, are those <base>_neigh.dat marks with -1 (ClNeigh, the
+    neighbour opposite vertex i; src/mod_cg_create_matrix.f90:645)."""
+    from oracle import gravity_ref
+    base = os.path.join(REF_DEMOS, model)
+    if not os.path.exists(base + "_neigh.dat"):
+        pytest.skip("reference demo models not present")
+    nt = int(open(base + "_mesh.header").read().split()[0])
+    ele = np.fromfile(base + "_ele.dat", dtype=np.int32).reshape(nt, 4) - 1
+    neigh = np.fromfile(base + "_neigh.dat", dtype=np.int32).reshape(nt, 4)
+    assert np.array_equal(gravity_ref.boundary_faces(ele), neigh == -1)
+
