@@ -1,7 +1,7 @@
 """A NormalModes job on the GPU: the reference's driver (src/mainnm.f90)
 with its configuration file and its result files, on this library.
 
-    python -m normalmodes_gb300.run global_conf [--mixed] [--block 0|32] [--dry-run]
+    python -m normalmodes_gb300.run global_conf [--mixed] [--block 0|32] [--slices N] [--dry-run]
 
 * ``global_conf`` is read as the reference reads it (para_init,
   src/mod_para.f90:79-137, with string_conf of src/mod_string.f90): on each
@@ -20,6 +20,9 @@ with its configuration file and its result files, on this library.
   src/mod_pevsl.f90:164-186), and the eigenvectors, the node list and the
   node status are written in the reference's files (nmm_write_results,
   src/mod_pevsl.f90:188-247).
+* ``--slices N`` cuts the interval into N slices of equal estimated
+  eigenvalue count (nm_slice_spectrum) and solves them on one context
+  (nm_solve_batched); the eigenpairs are merged in ascending order.
 * ``--dry-run`` stops before the GPU: configuration, model, assembly.
 """
 from __future__ import annotations
@@ -124,7 +127,27 @@ def make_solver(mats: dict, porder: int, mixed: bool):
     return Solver(mats, porder, precision=NM_PREC_MIXED if mixed else NM_PREC_FP64)
 
 
-def run(job: Job, mixed: bool = False, block: int | None = None, dry_run: bool = False, out=sys.stdout) -> dict:
+def _solve(sv, job: Job, block: int, slices: int, out):
+    """One interval (nm_solve), or `slices` slices of equal estimated
+    eigenvalue count (nm_slice_spectrum) solved on the same context
+    (nm_solve_batched) and merged in ascending order."""
+    if slices <= 1:
+        r = sv.solve(job.lowfreq, job.upfreq, want_vectors=True, unscale=True, block=block)
+        return r.lam, r.err_ref, r.vec
+    cuts, counts = sv.slice_spectrum(job.lowfreq, job.upfreq, slices)
+    print(" spectrum slices (mHz) and estimated eigenvalue counts:", file=out)
+    for (a, b), c in zip(cuts, counts):
+        print(f"   {a:.9f} {b:.9f} {c:10.1f}", file=out)
+    rs = sv.solve_batched(cuts, want_vectors=True, unscale=True, block=block)
+    lam = np.concatenate([r.lam for r in rs])
+    err = np.concatenate([r.err_ref for r in rs])
+    vec = np.concatenate([r.vec for r in rs], axis=1)
+    order = np.argsort(lam, kind="stable")
+    return lam[order], err[order], vec[:, order]
+
+
+def run(job: Job, mixed: bool = False, block: int | None = None, dry_run: bool = False, out=sys.stdout,
+        slices: int = 0) -> dict:
     from .model import Model
     model = Model.load(job.base_path, job.porder, gravity=job.gravity)
     info = model.info()
@@ -140,12 +163,12 @@ def run(job: Job, mixed: bool = False, block: int | None = None, dry_run: bool =
     if block is None:
         block = 32 if mixed else 0
     with make_solver(model.operators(), job.porder, mixed) as sv:
-        r = sv.solve(job.lowfreq, job.upfreq, want_vectors=True, unscale=True, block=block)
-    report(r.lam, r.err_ref, out=out)
+        lam, err, vec = _solve(sv, job, block, slices, out)
+    report(lam, err, out=out)
     os.makedirs(job.outputdir or ".", exist_ok=True)
-    prefix = model.write_results(job.outputdir, job.basename, job.lowfreq, job.upfreq, r.vec, job=job.job, nproc=1)
+    prefix = model.write_results(job.outputdir, job.basename, job.lowfreq, job.upfreq, vec, job=job.job, nproc=1)
     print(" save eigenvectors: " + prefix + "_<i>.dat", file=out)
-    summary.update(nev=len(r.lam), prefix=prefix, lam=r.lam)
+    summary.update(nev=len(lam), prefix=prefix, lam=lam)
     return summary
 
 
@@ -155,13 +178,15 @@ def main(argv=None) -> int:
     ap.add_argument("--mixed", action="store_true", help="mixed-precision block path")
     ap.add_argument("--block", type=int, default=None, help="0: single-vector, 32: block (default by precision)")
     ap.add_argument("--dry-run", action="store_true", help="read, load and assemble only")
+    ap.add_argument("--slices", type=int, default=0,
+                    help="solve N slices of equal estimated eigenvalue count on one context")
     a = ap.parse_args(argv)
     try:
         job = read_global_conf(a.conf)
     except ConfError as e:
         print(e, file=sys.stderr)
         return 2
-    run(job, mixed=a.mixed, block=a.block, dry_run=a.dry_run)
+    run(job, mixed=a.mixed, block=a.block, dry_run=a.dry_run, slices=a.slices)
     return 0
 
 

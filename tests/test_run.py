@@ -1,8 +1,9 @@
 """CPU tests of the job driver (python -m normalmodes_gb300.run): the
 reference's global_conf rules (src/mod_para.f90:79-137, src/mod_string.f90),
 dry runs over models in the reference's input files with and without the
-reference gravity, and a whole job whose GPU solve is replaced by the oracle
-(the printed tables and the result files)."""
+reference gravity, and whole jobs, single-interval and sliced, whose GPU
+context is replaced by the oracle (the printed tables and the result
+files)."""
 import io
 import os
 
@@ -103,6 +104,24 @@ class _OracleSolver:
         r.vec = r.Y * self.op.D[:, None] if unscale else r.Y
         return r
 
+    def slice_spectrum(self, lo, hi, n):
+        from normalmodes_gb300 import nmgpu
+        op = self.op
+        lmin, lmax, _ = self.O.lan_bounds(op.amv, op.n, 3000, 1e-5, solve=op.bsolve)
+        lmax += 0.005 * (lmax - lmin)
+        lam = [float(np.float32(f)) for f in (lo, hi)]
+        lam = [(2 * self.O.PI_REF * f) ** 2 * 1e-6 for f in lam]
+        deg = nmgpu.kpm_degree(lmin, lmax, lam[0], lam[1], n)
+
+        def apply(X):
+            return np.stack([op.bsolve(op.amv(X[:, j])) for j in range(X.shape[1])], axis=1)
+
+        mu = nmgpu.kpm_moments(apply, op.n, lmin, lmax, deg, nvec=8)
+        return nmgpu.kpm_slices(mu, op.n, lmin, lmax, lo, hi, n)
+
+    def solve_batched(self, cuts, want_vectors, unscale, block):
+        return [self.solve(a, b, want_vectors, unscale, block) for a, b in cuts]
+
 
 def test_whole_job_with_a_stand_in_solver(tmp_path, monkeypatch):
     from oracle import oracle as O
@@ -123,3 +142,18 @@ def test_whole_job_with_a_stand_in_solver(tmp_path, monkeypatch):
     assert vec1.size == s["n"]
     assert os.path.exists(str(tmp_path / "output" / "ball.1_pod1_np1_vlist.dat"))
     assert not os.path.exists(prefix + f"_{s['nev'] + 1}.dat")
+
+
+def test_sliced_job_matches_the_single_interval(tmp_path, monkeypatch):
+    """--slices: KPM slices solved one after another and merged give the
+    eigenvalues of the single-interval solve."""
+    conf = _job_files(tmp_path, 2)
+    monkeypatch.setattr(R, "make_solver", _OracleSolver)
+    whole = R.run(R.read_global_conf(conf), out=io.StringIO())
+    out = io.StringIO()
+    sliced = R.run(R.read_global_conf(conf), out=out, slices=3)
+    assert "spectrum slices" in out.getvalue()
+    assert sliced["nev"] == whole["nev"]
+    assert np.max(np.abs(sliced["lam"] - whole["lam"]) / whole["lam"]) < 1e-10
+    assert np.all(np.diff(sliced["lam"]) >= 0)
+
