@@ -109,7 +109,9 @@ typedef struct nm_ctx nm_ctx;
  * Solid-only model: A = stiffness, Ap = E = ET = NULL.  Fluid-solid model:
  * A = Ad, plus Ap (reference sign, negative definite), E, ET.  The library
  * computes D = diag(B)^-1/2, D_p = diag(-Ap)^-1/2, the scaled operators, the
- * Lanczos bounds of B_s and Ap_s and the Chebyshev set-ups itself. */
+ * Lanczos bounds of B_s and Ap_s and the Chebyshev set-ups itself.
+ * *out is set in every case but a NULL out: on failure it holds the context
+ * with the error message (nm_last_error), and the caller calls nm_destroy. */
 int nm_create(nm_ctx** out, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, const nm_csr* E,
               const nm_csr* ET, const nm_opts* opts);
 void nm_destroy(nm_ctx* ctx);
