@@ -1,7 +1,7 @@
 """Time the eigensolver's operators on a synthetic layered ball.
 
     python -m normalmodes_gb300.timeop [--cells 36] [--porder 2] [--lateral 0]
-                                       [--precision mixed|fp64] [--ops 4,5,6] [--reps 5]
+                                       [--precision mixed|fp64] [--ops 4,5,6] [--reps 5] [--gravity]
 
 Operators (nm_time_op): 0 A-op, 1 B SpMV, 2 B Chebyshev solve, 3 one filter
 degree step (single vector, FP64 SELL); 4 block mass Chebyshev solve, 5
@@ -25,6 +25,7 @@ def main(argv=None) -> None:
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--ops", default="4,5,6")
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--gravity", action="store_true", help="operators with the reference gravity (JOB = 2)")
     a = ap.parse_args(argv)
     from normalmodes_gb300.model import Model
     from normalmodes_gb300.nmgpu import NM_PREC_FP64, NM_PREC_MIXED, Solver
@@ -32,7 +33,7 @@ def main(argv=None) -> None:
     if a.lateral > 0:
         kw.update(lateral_pert=a.lateral, lateral_lmax=8)
     t = time.perf_counter()
-    m = Model.ball(**kw)
+    m = Model.ball(gravity=a.gravity, **kw)
     mats = m.operators()
     t_model = time.perf_counter() - t
     with Solver(mats, a.porder, precision=NM_PREC_MIXED if a.precision == "mixed" else NM_PREC_FP64) as sv:
