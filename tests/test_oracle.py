@@ -62,3 +62,44 @@ def test_homogeneous_ball_matches_the_analytic_sphere():
         assert rel.max() < tol, (nc, rel.max())
         mean[nc] = rel.mean()
     assert mean[8] < 0.6 * mean[6]
+
+
+@pytest.mark.parametrize("name", ["solid_p1", "fs_p1", "fs_p2"])
+def test_oracle_operators_match_sparse_algebra(small_models, name):
+    """The C oracle's operators against scipy: D = diag(B)^-1/2 and
+    D_p = diag(-Ap)^-1/2 (src/mod_matvec.f90:252-441), B_s x, the solid
+    A_s x, and for fluid-solid models D (Ad - E Ap^-1 ET) D x with the exact
+    Ap^-1, within the Golub-Varga bound 2 sigma^d of the Chebyshev Ap solve;
+    the Chebyshev B solve recovers x from B_s x within 2 sigma^d sqrt(kappa)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+
+    from oracle import oracle as O
+    d = small_models[name]
+    mats = d["mats"]
+    op = O.setup_operator(mats, d["porder"])
+    B = mats["B"].to_scipy()
+    D = 1.0 / np.sqrt(B.diagonal())
+    assert np.max(np.abs(op.D - D)) <= 1e-15 * np.max(D)
+    Bs = sp.diags(D) @ B @ sp.diags(D)
+    x = np.random.default_rng(0).standard_normal(op.n)
+    bx = Bs @ x
+    assert np.max(np.abs(op.bmv(x) - bx)) <= 1e-14 * np.max(np.abs(bx))
+
+    def bound(cheb):
+        lo, hi, deg = cheb
+        k = hi / lo
+        return 2.0 * ((np.sqrt(k) - 1) / (np.sqrt(k) + 1)) ** deg, k
+
+    eb, kb = bound(op.b_cheb)
+    assert np.linalg.norm(op.bsolve(bx) - x) <= eb * np.sqrt(kb) * np.linalg.norm(x)
+    if "Ad" in mats:
+        Ap = mats["Ap"].to_scipy()
+        assert np.max(np.abs(op.Dp - 1.0 / np.sqrt(-Ap.diagonal()))) <= 1e-15 * np.max(op.Dp)
+        Ad, E, ET = (mats[k].to_scipy() for k in ("Ad", "E", "ET"))
+        exact = D * (Ad @ (D * x) - E @ sla.spsolve(Ap.tocsc(), ET @ (D * x)))
+        ea, _ = bound(op.ap_cheb)
+        assert np.max(np.abs(op.amv(x) - exact)) <= (ea + 1e-13) * np.max(np.abs(exact))
+    else:
+        ax = D * (mats["A"].to_scipy() @ (D * x))
+        assert np.max(np.abs(op.amv(x) - ax)) <= 1e-14 * np.max(np.abs(ax))
