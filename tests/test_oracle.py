@@ -103,3 +103,36 @@ def test_oracle_operators_match_sparse_algebra(small_models, name):
     else:
         ax = D * (mats["A"].to_scipy() @ (D * x))
         assert np.max(np.abs(op.amv(x) - ax)) <= 1e-14 * np.max(np.abs(ax))
+
+
+@pytest.mark.parametrize("xintv", [
+    [0.2, 0.3, 0.0, 1.0], [3.9e-7, 1.58e-4, -1e-9, 0.6], [1.579e-6, 3.9478e-5, -5e-9, 1.475e-3],
+    [0.5, 0.9, 0.0, 1.0], [0.0, 0.05, 0.0, 1.0], [0.9, 1.0, 0.0, 1.0],
+])
+def test_filter_design_rule(xintv):
+    """The filter of pEVSL_FINDPOL_F90 (src/mod_pevsl.f90:108-115) as the
+    oracle designs it: p(gamma) = 1; an interior filter is balanced,
+    p(a) = p(b); the bar is at or below the threshold (0.8 interior, 0.7 for
+    an end interval) and the degree is the smallest that reaches it; on a
+    fine grid p stays at or above the bar inside [a, b] and below it
+    outside, which is what keeping Ritz values with p(theta) > bar relies on."""
+    from oracle import oracle as O
+    p = O.find_pol(xintv)
+    a, b, lmin, lmax = xintv
+
+    def ev(x):
+        return O._cheb_eval(p.mu, (x - p.cc) / p.dd)
+
+    assert abs(O._cheb_eval(p.mu, p.gam) - 1.0) < 1e-12
+    thresh = 0.8 if p.kind == "interior" else 0.7
+    assert p.bar <= thresh
+    if p.kind == "interior":
+        assert abs(ev(a) - ev(b)) < 1e-10
+    if p.deg > 2:
+        q = O.find_pol(xintv, min_deg=p.deg - 1, max_deg=p.deg - 1)
+        assert q.bar > thresh
+    xs = np.linspace(lmin, lmax, 20001)
+    inside = np.array([ev(x) for x in xs if a <= x <= b])
+    outside = np.array([ev(x) for x in xs if x < a or x > b])
+    assert inside.min() >= p.bar - 1e-12
+    assert outside.max() < p.bar
