@@ -136,3 +136,28 @@ def test_filter_design_rule(xintv):
     outside = np.array([ev(x) for x in xs if x < a or x > b])
     assert inside.min() >= p.bar - 1e-12
     assert outside.max() < p.bar
+
+
+@pytest.mark.parametrize("name", ["solid_p1", "fs_p1"])
+def test_lanczos_bounds_bracket_the_spectra(small_models, name):
+    """pEVSL_LANBOUNDS_F90 (src/mod_pevsl.f90:84) as the oracle restates it:
+    the bounds of B^-1 A, B_s and Ap_s against dense spectra, to 1e-8 of the
+    spectral width (the filter and the Chebyshev set-ups only need that)."""
+    from scipy.linalg import eigh, eigvalsh
+
+    from oracle import oracle as O
+    d = small_models[name]
+    op = O.setup_operator(d["mats"], d["porder"])
+    A, Bm = O.dense_operator(op)
+    w = eigh(A, Bm, eigvals_only=True)
+    lo, hi, _ = O.lan_bounds(op.amv, op.n, 3000, 1e-5, solve=op.bsolve)
+    width = w[-1] - w[0]
+    assert lo <= w[0] + 1e-8 * width and abs(hi - w[-1]) <= 1e-8 * width
+    wb = eigvalsh(Bm)
+    blo, bhi = op.bounds["B"]
+    assert abs(blo - wb[0]) <= 1e-8 * wb[-1] and abs(bhi - wb[-1]) <= 1e-8 * wb[-1]
+    if "Ap" in op.bounds:
+        Ap = d["mats"]["Ap"].to_scipy().toarray()
+        wa = eigvalsh(op.Dp[:, None] * (-Ap) * op.Dp[None, :])
+        alo, ahi = op.bounds["Ap"]
+        assert abs(alo - wa[0]) <= 1e-8 * wa[-1] and abs(ahi - wa[-1]) <= 1e-8 * wa[-1]
