@@ -40,6 +40,8 @@ int check_csr(nm_ctx* c, const nm_csr* m, int nr, int nc, const char* name) {
   const long long nnz = m->rowptr[nr];
   for (long long q = 0; q < nnz; ++q)
     if (m->col[q] < 0 || m->col[q] >= nc) return set_err(c, NM_ERR_ARG, std::string("column out of range in ") + name);
+  for (long long q = 0; q < nnz; ++q)
+    if (!std::isfinite(m->val[q])) return set_err(c, NM_ERR_NUMERIC, std::string("non-finite value in ") + name);
   return NM_OK;
 }
 

@@ -102,3 +102,34 @@ def test_bad_arguments_rejected(small_models):
     with pytest.raises(nmgpu.NmError) as ei:
         nmgpu.Solver(mats, d["porder"])
     assert ei.value.code == -1  # NM_ERR_ARG
+
+
+@pytest.mark.parametrize("which,fault,code", [
+    ("B", "rowptr0", -1), ("Ad", "rowptr_order", -1), ("E", "col_range", -1),
+    ("Ad", "nan", -6), ("ET", "inf", -6), ("Ap", "nan", -6),
+])
+def test_corrupted_inputs_rejected_on_the_host(small_models, which, fault, code):
+    """Host-side fault injection: corrupted CSR (NM_ERR_ARG) and NaN / Inf
+    values (NM_ERR_NUMERIC) planted in host copies of the operators are
+    rejected by nm_create's validator before any device work, so the codes
+    are the same with or without a GPU."""
+    import copy
+    d = small_models["fs_p1"]
+    mats = dict(d["mats"])
+    m = copy.deepcopy(mats[which])
+    if fault == "rowptr0":
+        m.rowptr = m.rowptr.copy()
+        m.rowptr[0] = 1
+    elif fault == "rowptr_order":
+        m.rowptr = m.rowptr.copy()
+        m.rowptr[5], m.rowptr[6] = m.rowptr[6], m.rowptr[5] - 1
+    elif fault == "col_range":
+        m.col = m.col.copy()
+        m.col[7] = m.shape[1]
+    else:
+        m.val = m.val.copy()
+        m.val[len(m.val) // 2] = np.nan if fault == "nan" else np.inf
+    mats[which] = m
+    with pytest.raises(nmgpu.NmError) as ei:
+        nmgpu.Solver(mats, d["porder"])
+    assert ei.value.code == code
