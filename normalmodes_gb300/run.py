@@ -19,7 +19,9 @@ with its configuration file and its result files, on this library.
   (relative errors, then frequencies in mHz and periods in s,
   src/mod_pevsl.f90:164-186), and the eigenvectors, the node list and the
   node status are written in the reference's files (nmm_write_results,
-  src/mod_pevsl.f90:188-247).
+  src/mod_pevsl.f90:188-247), with a JSON run record beside them
+  (``<prefix>_run.json``: configuration, sizes, per slice the filter degree,
+  Lanczos steps, timings and operator counts, per eigenpair both residuals).
 * ``--slices N`` cuts the interval into N slices of equal estimated
   eigenvalue count (nm_slice_spectrum) and solves them on one context
   (nm_solve_batched); the eigenpairs are merged in ascending order.
@@ -28,6 +30,7 @@ with its configuration file and its result files, on this library.
 from __future__ import annotations
 
 import argparse
+import json
 import math
 import os
 import sys
@@ -132,18 +135,45 @@ def _solve(sv, job: Job, block: int, slices: int, out):
     eigenvalue count (nm_slice_spectrum) solved on the same context
     (nm_solve_batched) and merged in ascending order."""
     if slices <= 1:
-        r = sv.solve(job.lowfreq, job.upfreq, want_vectors=True, unscale=True, block=block)
-        return r.lam, r.err_ref, r.vec
-    cuts, counts = sv.slice_spectrum(job.lowfreq, job.upfreq, slices)
-    print(" spectrum slices (mHz) and estimated eigenvalue counts:", file=out)
-    for (a, b), c in zip(cuts, counts):
-        print(f"   {a:.9f} {b:.9f} {c:10.1f}", file=out)
-    rs = sv.solve_batched(cuts, want_vectors=True, unscale=True, block=block)
+        cuts, counts = [(job.lowfreq, job.upfreq)], [None]
+        rs = [sv.solve(job.lowfreq, job.upfreq, want_vectors=True, unscale=True, block=block)]
+    else:
+        cuts, counts = sv.slice_spectrum(job.lowfreq, job.upfreq, slices)
+        print(" spectrum slices (mHz) and estimated eigenvalue counts:", file=out)
+        for (a, b), c in zip(cuts, counts):
+            print(f"   {a:.9f} {b:.9f} {c:10.1f}", file=out)
+        rs = sv.solve_batched(cuts, want_vectors=True, unscale=True, block=block)
     lam = np.concatenate([r.lam for r in rs])
     err = np.concatenate([r.err_ref for r in rs])
+    res2 = np.concatenate([r.res2 for r in rs])
     vec = np.concatenate([r.vec for r in rs], axis=1)
     order = np.argsort(lam, kind="stable")
-    return lam[order], err[order], vec[:, order]
+    meta = [{"f_lo_mhz": float(a), "f_hi_mhz": float(b), "estimated_count": None if c is None else float(c),
+             "nev": int(len(r.lam)), "xintv": [float(x) for x in r.xintv], "filter_degree": int(r.pol_deg),
+             "lanczos_steps": int(r.lanczos_steps), "times_s": {k: float(v) for k, v in r.times.items()},
+             "operator_counts": {k: int(v) for k, v in r.counts.items()}}
+            for (a, b), c, r in zip(cuts, counts, rs)]
+    return lam[order], err[order], res2[order], vec[:, order], meta
+
+
+def run_record(job: Job, model, mixed: bool, block: int, lam, err, res2, meta) -> dict:
+    """The JSON run record: configuration, model sizes, solver settings, per
+    slice the interval, filter, steps, timings and operator counts, and per
+    eigenpair its eigenvalue, frequency, period and both residual norms."""
+    info = model.info()
+    nnz = dict(zip(("A", "B", "Ad", "Ap", "E", "ET"), (int(x) for x in info.nnz)))
+    pos = lam > 1e-15
+    f = np.where(pos, np.sqrt(np.abs(lam)) / PI / 2.0 * 1e3, 0.0)
+    T = np.where(pos, 2.0 * PI / np.sqrt(np.where(pos, lam, 1.0)), 0.0)
+    return {
+        "config": {"JOB": job.job, "basename": job.basename, "inputdir": job.inputdir, "outputdir": job.outputdir,
+                   "lowfreq": job.lowfreq, "upfreq": job.upfreq, "pOrder": job.porder},
+        "model": {"ntet": info.ntet, "n_fluid_tets": info.n_fluid_tets, "n": info.n, "np": info.np,
+                  "nnz": {k: v for k, v in nnz.items() if v}, "gravity": job.gravity},
+        "solver": {"precision": "mixed" if mixed else "fp64", "block": block, "slices": meta},
+        "eigenpairs": {"lambda": lam.tolist(), "f_mhz": f.tolist(), "period_s": T.tolist(),
+                       "err_ref": err.tolist(), "res2": res2.tolist()},
+    }
 
 
 def run(job: Job, mixed: bool = False, block: int | None = None, dry_run: bool = False, out=sys.stdout,
@@ -163,11 +193,14 @@ def run(job: Job, mixed: bool = False, block: int | None = None, dry_run: bool =
     if block is None:
         block = 32 if mixed else 0
     with make_solver(model.operators(), job.porder, mixed) as sv:
-        lam, err, vec = _solve(sv, job, block, slices, out)
+        lam, err, res2, vec, meta = _solve(sv, job, block, slices, out)
     report(lam, err, out=out)
     os.makedirs(job.outputdir or ".", exist_ok=True)
     prefix = model.write_results(job.outputdir, job.basename, job.lowfreq, job.upfreq, vec, job=job.job, nproc=1)
     print(" save eigenvectors: " + prefix + "_<i>.dat", file=out)
+    with open(prefix + "_run.json", "w") as f:
+        json.dump(run_record(job, model, mixed, block, lam, err, res2, meta), f, indent=1)
+    print(" run record: " + prefix + "_run.json", file=out)
     summary.update(nev=len(lam), prefix=prefix, lam=lam)
     return summary
 

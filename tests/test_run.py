@@ -100,9 +100,11 @@ class _OracleSolver:
         return False
 
     def solve(self, lo, hi, want_vectors, unscale, block):
+        from types import SimpleNamespace
         r = self.O.apply_pevsl(self.op, lo, hi)
-        r.vec = r.Y * self.op.D[:, None] if unscale else r.Y
-        return r
+        return SimpleNamespace(lam=r.lam, vec=r.Y * self.op.D[:, None] if unscale else r.Y, err_ref=r.err_ref,
+                               res2=r.res2, xintv=tuple(r.xintv), pol_deg=r.pol.deg, lanczos_steps=r.steps,
+                               times=dict(r.times), counts={"amv": self.op.nmatvec["A"]})
 
     def slice_spectrum(self, lo, hi, n):
         from normalmodes_gb300 import nmgpu
@@ -142,6 +144,12 @@ def test_whole_job_with_a_stand_in_solver(tmp_path, monkeypatch):
     assert vec1.size == s["n"]
     assert os.path.exists(str(tmp_path / "output" / "ball.1_pod1_np1_vlist.dat"))
     assert not os.path.exists(prefix + f"_{s['nev'] + 1}.dat")
+    import json
+    rec = json.load(open(prefix + "_run.json"))
+    assert rec["config"]["JOB"] == 2 and rec["model"]["gravity"] and rec["model"]["n"] == s["n"]
+    assert np.allclose(rec["eigenpairs"]["lambda"], s["lam"]) and np.allclose(rec["eigenpairs"]["f_mhz"], f)
+    sl = rec["solver"]["slices"]
+    assert len(sl) == 1 and sl[0]["nev"] == s["nev"] and sl[0]["filter_degree"] > 0
 
 
 def test_sliced_job_matches_the_single_interval(tmp_path, monkeypatch):
