@@ -23,15 +23,21 @@ SellHost sell_from_csr(const nm_csr* m, const double* dl, const double* dr, doub
   h.nnz = m->rowptr[m->nrows];
   h.slice_ptr.assign(h.nslices + 1, 0);
   h.row_len.resize(m->nrows);
+  // Every row fills its own slots, so rows (and slices) are packed in
+  // parallel; the result does not depend on the thread count.
+#pragma omp parallel for schedule(static)
   for (int r = 0; r < m->nrows; ++r) h.row_len[r] = m->rowptr[r + 1] - m->rowptr[r];
+#pragma omp parallel for schedule(static)
   for (int s = 0; s < h.nslices; ++s) {
     int w = 0;
     for (int r = s * kSlice; r < std::min(m->nrows, (s + 1) * kSlice); ++r) w = std::max(w, h.row_len[r]);
-    h.slice_ptr[s + 1] = h.slice_ptr[s] + (long long)w * kSlice;
+    h.slice_ptr[s + 1] = (long long)w * kSlice;
   }
+  for (int s = 0; s < h.nslices; ++s) h.slice_ptr[s + 1] += h.slice_ptr[s];
   h.nstored = h.slice_ptr[h.nslices];
   h.col.assign(h.nstored, 0);
   h.val.assign(h.nstored, 0.0);
+#pragma omp parallel for schedule(dynamic, 1024)
   for (int r = 0; r < m->nrows; ++r) {
     const long long base = h.slice_ptr[r / kSlice] + (r % kSlice);
     for (int k = 0; k < h.row_len[r]; ++k) {
@@ -412,6 +418,16 @@ long long nm_test_sell(int nrows, int ncols, const int* rowptr, const int* col, 
   std::copy(h.row_len.begin(), h.row_len.end(), row_len);
   std::copy(h.slice_ptr.begin(), h.slice_ptr.end(), slice_ptr);
   return h.nstored;
+}
+
+// SELL packing with scaling: the packed column indices and values
+// (nstored each, returned by nm_test_sell for the same matrix).
+void nm_test_sell_arrays(int nrows, int ncols, const int* rowptr, const int* col, const double* val,
+                         const double* dl, const double* dr, double sign, int* col_out, double* val_out) {
+  nm_csr m{nrows, ncols, rowptr, col, val};
+  nmg::SellHost h = nmg::sell_from_csr(&m, dl, dr, sign);
+  std::copy(h.col.begin(), h.col.end(), col_out);
+  std::copy(h.val.begin(), h.val.end(), val_out);
 }
 
 void nm_test_start_vector(int n, double* out) {

@@ -197,6 +197,8 @@ def lib() -> C.CDLL:
                                    C.POINTER(C.c_int), C.POINTER(C.c_longlong)]
         L.nm_test_sell.restype = C.c_longlong
         L.nm_test_start_vector.argtypes = [C.c_int, dp]
+        L.nm_test_sell_arrays.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), dp, dp, dp,
+                                          C.c_double, C.POINTER(C.c_int), dp]
         L.nm_default_kpm_opts.argtypes = [C.POINTER(NmKpmOpts)]
         L.nm_kpm_degree.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
         L.nm_kpm_moments.argtypes = [NM_BLOCK_OP, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,

@@ -21,6 +21,13 @@ def test_exports_every_declared_symbol():
     missing = [s for s in sorted(declared) if not hasattr(L, s)]
     assert not missing, missing
     assert set(nmgpu.EXPORTS) <= declared
+    # and the model library exports what include/nmmodel.h declares
+    from normalmodes_gb300 import model
+    mh = open(os.path.join(ROOT, "include", "nmmodel.h")).read()
+    mdecl = set(re.findall(r"\b(nmm_[a-z_0-9]+)\s*\(", mh))
+    assert {"nmm_set_gravity", "nmm_load_gravity", "nmm_ball_gravity", "nmm_get_gravity"} <= mdecl
+    ML = model.lib()
+    assert not [f for f in sorted(mdecl) if not hasattr(ML, f)]
 
 
 def test_start_vector_matches_oracle():
@@ -79,6 +86,54 @@ def test_sell_packing():
     assert np.array_equal(rl, lens)
     widths = [lens[s * 32:(s + 1) * 32].max() for s in range(len(sp) - 1)]
     assert stored == 32 * sum(widths) == sp[-1]
+
+
+def _sell_reference(rp, col, val, dl, dr, sign, S=32):
+    """SELL-S layout: slices of S rows padded to their longest row, stored
+    column-major within a slice; padding repeats the row's last column with
+    value 0; values scaled as sign * dl[r] * a_rc * dr[c]."""
+    nr = len(rp) - 1
+    lens = np.diff(rp)
+    ns = (nr + S - 1) // S
+    width = [int(lens[s * S:(s + 1) * S].max()) for s in range(ns)]
+    ptr = np.concatenate([[0], np.cumsum(np.array(width) * S)])
+    C_ = np.zeros(ptr[-1], np.int32)
+    V = np.zeros(ptr[-1])
+    for r in range(nr):
+        base = ptr[r // S] + r % S
+        cols = col[rp[r]:rp[r + 1]]
+        vals = sign * val[rp[r]:rp[r + 1]] * dr[cols] * dl[r]
+        for k in range(width[r // S]):
+            C_[base + k * S] = cols[k] if k < len(cols) else (cols[-1] if len(cols) else 0)
+            V[base + k * S] = vals[k] if k < len(cols) else 0.0
+    return C_, V
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_sell_arrays_match_the_layout(seed):
+    """The packed indices and scaled values (what nm_create uploads) against a
+    direct restatement of the layout, element for element; empty rows and a
+    ragged last slice included."""
+    import ctypes as C
+    rng = np.random.default_rng(seed)
+    nr, nc = 1000 + 37 * seed, 300
+    lens = rng.integers(0, 12, size=nr)
+    lens[rng.integers(0, nr, 20)] = 0
+    rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    col = rng.integers(0, nc, size=rp[-1]).astype(np.int32)
+    val = rng.standard_normal(rp[-1])
+    dl, dr = rng.uniform(0.5, 2.0, nr), rng.uniform(0.5, 2.0, nc)
+    L = nmgpu.lib()
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    rl = np.zeros(nr, np.int32)
+    sp = np.zeros((nr + 31) // 32 + 1, np.int64)
+    stored = L.nm_test_sell(nr, nc, ip(rp), ip(col), fp(val), ip(rl), sp.ctypes.data_as(C.POINTER(C.c_longlong)))
+    Cg, Vg = np.zeros(stored, np.int32), np.zeros(stored)
+    L.nm_test_sell_arrays(nr, nc, ip(rp), ip(col), fp(val), fp(dl), fp(dr), -1.0, ip(Cg), fp(Vg))
+    Cr, Vr = _sell_reference(rp, col, val, dl, dr, -1.0)
+    assert np.array_equal(Cg, Cr)
+    assert np.array_equal(Vg, Vr)
 
 
 def test_no_gpu_fails_loudly(small_models):
