@@ -142,10 +142,21 @@ int nm_kpm_moments(nm_block_op op, void* data, int n, double lmin, double lmax, 
   for (int j = 0; j < nvec; ++j)
     for (int i = 0; i < n; ++i)
       V[(size_t)j * n + i] = (mix64(seed * 0x100000001B3ull + (uint64_t)j * (uint64_t)n + (uint64_t)i) >> 63) ? 1.0 : -1.0;
+  // v'w as partial sums over fixed chunks added in order: the moments, and
+  // with them the slices, do not depend on the thread count.
+  constexpr long long kChunk = 1 << 16;
+  const long long nchunk = ((long long)len + kChunk - 1) / kChunk;
+  std::vector<double> part(nchunk);
   auto dot = [&](const std::vector<double>& W) {
+#pragma omp parallel for schedule(static)
+    for (long long b = 0; b < nchunk; ++b) {
+      double s = 0.0;
+      const long long e = std::min((long long)len, (b + 1) * kChunk);
+      for (long long i = b * kChunk; i < e; ++i) s += V[i] * W[i];
+      part[b] = s;
+    }
     double s = 0.0;
-#pragma omp parallel for reduction(+ : s) schedule(static)
-    for (long long i = 0; i < (long long)len; ++i) s += V[i] * W[i];
+    for (long long b = 0; b < nchunk; ++b) s += part[b];
     return s;
   };
   int rc;

@@ -2,6 +2,9 @@
 recurrence, the weighted count and the slices, driven through the block
 operator callback by exact diagonal operators and by the oracle's B^-1 A."""
 import math
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -104,3 +107,21 @@ def test_bad_arguments():
 
     with pytest.raises(ValueError, match="operator failed"):
         nmgpu.kpm_moments(broken, 10, 0.0, 1.0, 3, 2)  # operator errors surface
+
+
+def test_moments_do_not_depend_on_the_thread_count():
+    """Bitwise-identical moments with 1 and 4 OpenMP threads (fixed-chunk
+    partial sums), so the slices are the same on any host."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = (
+        "import sys, numpy as np; sys.path.insert(0, %r)\n"
+        "from normalmodes_gb300 import nmgpu\n"
+        "rng = np.random.default_rng(1); lam = rng.uniform(0, 1, 300000)\n"
+        "mu = nmgpu.kpm_moments(lambda X: lam[:, None] * X, len(lam), 0.0, 1.0, 30, nvec=2)\n"
+        "sys.stdout.write(mu.tobytes().hex())\n" % root)
+    outs = []
+    for nt in ("1", "4"):
+        env = dict(os.environ, OMP_NUM_THREADS=nt)
+        outs.append(subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env,
+                                   check=True, timeout=300).stdout)
+    assert outs[0] == outs[1] and len(outs[0]) > 0
