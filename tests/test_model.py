@@ -185,3 +185,24 @@ def test_write_results_reference_layout(tmp_path):
     assert vlist[vert_nodes].max() == info.nvert
     vstat = np.fromfile(tmp_path / "ball_pod2_np1_vstat.dat", dtype=np.int32)
     assert vstat.size == info.nnode and vstat.min() >= 0 and vstat.max() <= 5
+
+
+def test_assembly_does_not_depend_on_the_thread_count():
+    """Bitwise-identical operators with 1 and 4 OpenMP threads (elements in
+    parallel, scatter in element order), with and without gravity."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = (
+        "import sys, hashlib; sys.path.insert(0, %r)\n"
+        "from normalmodes_gb300.model import Model\n"
+        "h = hashlib.sha256()\n"
+        "for g in (False, True):\n"
+        "    m = Model.ball(n_cells=8, porder=2, gravity=g)\n"
+        "    for k, c in sorted(m.operators().items()):\n"
+        "        h.update(c.rowptr.tobytes()); h.update(c.col.tobytes()); h.update(c.val.tobytes())\n"
+        "sys.stdout.write(h.hexdigest())\n" % root)
+    outs = [subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, check=True, timeout=300,
+                           env=dict(os.environ, OMP_NUM_THREADS=nt)).stdout for nt in ("1", "4")]
+    assert outs[0] == outs[1] and len(outs[0]) == 64
