@@ -7,8 +7,9 @@ Everything is compiled in-tree with plain compiler invocations (no cmake):
 * ``libnmgpu.so``   -- CUDA for sm_103a (nvcc): the GPU eigensolver behind the
   C-ABI declared in ``include/nmgpu.h``.
 
-The oracle under ``oracle/`` has its own recipe (``oracle/build.py``) because
-it is test infrastructure, not part of the product.
+The oracle under ``oracle/`` has its own recipe (``oracle.build()`` in
+``oracle/oracle.py``) because it is test infrastructure, not part of the
+product.
 """
 from __future__ import annotations
 
