@@ -105,6 +105,12 @@ class Csr:
         return sp.csr_matrix((self.val, self.col, self.rowptr), shape=self.shape)
 
 
+def write_vector(path: str, x) -> None:
+    """One raw float64 vector file, as the reference writes eigenvectors."""
+    a = np.ascontiguousarray(x, dtype=np.float64)
+    _check(lib().nmm_write_vector(path.encode(), a.ctypes.data_as(C.POINTER(C.c_double)), a.size))
+
+
 def default_opts(**kw) -> BallOpts:
     o = BallOpts()
     lib().nmm_ball_default_opts(C.byref(o))

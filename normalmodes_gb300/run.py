@@ -30,6 +30,7 @@ with its configuration file and its result files, on this library.
 from __future__ import annotations
 
 import argparse
+import io
 import json
 import math
 import os
@@ -123,37 +124,87 @@ def report(lam, err, out=sys.stdout) -> None:
     print(" " + "=" * 64, file=out)
 
 
-def make_solver(mats: dict, porder: int, mixed: bool):
+def make_solver(mats: dict, porder: int, mixed: bool, device: int = 0):
     """The GPU context for the job's operators (fails without the CUDA
     library or a GPU; there is no CPU path)."""
     from .nmgpu import NM_PREC_FP64, NM_PREC_MIXED, Solver
-    return Solver(mats, porder, precision=NM_PREC_MIXED if mixed else NM_PREC_FP64)
+    return Solver(mats, porder, device=device, precision=NM_PREC_MIXED if mixed else NM_PREC_FP64)
 
 
-def _solve(sv, job: Job, block: int, slices: int, out):
+class Group:
+    """The ranks of a job started by torchrun, one GPU each (RANK,
+    WORLD_SIZE and LOCAL_RANK from the environment; MASTER_ADDR/PORT for the
+    rendezvous).  Only small control messages cross ranks -- the slices,
+    eigenvalues and file indices -- so they go over gloo.  Without torchrun
+    it is a single rank and nothing is imported."""
+
+    def __init__(self):
+        self.size = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self._own = False
+        if self.size > 1:
+            import torch.distributed as dist
+            if not dist.is_initialized():
+                os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+                dist.init_process_group("gloo", rank=self.rank, world_size=self.size)
+                self._own = True
+
+    def bcast(self, obj):
+        if self.size == 1:
+            return obj
+        import torch.distributed as dist
+        box = [obj]
+        dist.broadcast_object_list(box, src=0)
+        return box[0]
+
+    def gather(self, obj) -> list:
+        if self.size == 1:
+            return [obj]
+        import torch.distributed as dist
+        out = [None] * self.size
+        dist.all_gather_object(out, obj)
+        return out
+
+    def close(self) -> None:
+        if self._own:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+            self._own = False
+
+
+def _solve(sv, job: Job, block: int, slices: int, out, grp: Group):
     """One interval (nm_solve), or `slices` slices of equal estimated
-    eigenvalue count (nm_slice_spectrum) solved on the same context
-    (nm_solve_batched) and merged in ascending order."""
+    eigenvalue count (nm_slice_spectrum, on the first rank) solved on this
+    rank's context (nm_solve_batched): slice j belongs to rank j mod size.
+    Returns this rank's eigenpairs in ascending order and per-slice records."""
     if slices <= 1:
-        cuts, counts = [(job.lowfreq, job.upfreq)], [None]
+        cuts, counts, mine = [(job.lowfreq, job.upfreq)], [None], [0]
         rs = [sv.solve(job.lowfreq, job.upfreq, want_vectors=True, unscale=True, block=block)]
     else:
-        cuts, counts = sv.slice_spectrum(job.lowfreq, job.upfreq, slices)
+        cuts, counts = grp.bcast(sv.slice_spectrum(job.lowfreq, job.upfreq, slices) if grp.rank == 0 else None)
         print(" spectrum slices (mHz) and estimated eigenvalue counts:", file=out)
-        for (a, b), c in zip(cuts, counts):
-            print(f"   {a:.9f} {b:.9f} {c:10.1f}", file=out)
-        rs = sv.solve_batched(cuts, want_vectors=True, unscale=True, block=block)
-    lam = np.concatenate([r.lam for r in rs])
-    err = np.concatenate([r.err_ref for r in rs])
-    res2 = np.concatenate([r.res2 for r in rs])
-    vec = np.concatenate([r.vec for r in rs], axis=1)
+        for j, ((a, b), c) in enumerate(zip(cuts, counts)):
+            print(f"   {a:.9f} {b:.9f} {c:10.1f}   rank {j % grp.size}", file=out)
+        mine = [j for j in range(len(cuts)) if j % grp.size == grp.rank]
+        rs = sv.solve_batched([cuts[j] for j in mine], want_vectors=True, unscale=True, block=block) if mine else []
+    if rs:
+        lam = np.concatenate([r.lam for r in rs])
+        err = np.concatenate([r.err_ref for r in rs])
+        res2 = np.concatenate([r.res2 for r in rs])
+        vs = [r.vec for r in rs if r.vec is not None and r.vec.size]
+        vec = np.concatenate(vs, axis=1) if vs else np.zeros((0, 0))
+    else:
+        lam = err = res2 = np.zeros(0)
+        vec = np.zeros((0, 0))
     order = np.argsort(lam, kind="stable")
-    meta = [{"f_lo_mhz": float(a), "f_hi_mhz": float(b), "estimated_count": None if c is None else float(c),
-             "nev": int(len(r.lam)), "xintv": [float(x) for x in r.xintv], "filter_degree": int(r.pol_deg),
+    meta = [{"slice": j, "rank": grp.rank, "f_lo_mhz": float(cuts[j][0]), "f_hi_mhz": float(cuts[j][1]),
+             "estimated_count": None if counts[j] is None else float(counts[j]), "nev": int(len(r.lam)),
+             "xintv": [float(x) for x in r.xintv], "filter_degree": int(r.pol_deg),
              "lanczos_steps": int(r.lanczos_steps), "times_s": {k: float(v) for k, v in r.times.items()},
              "operator_counts": {k: int(v) for k, v in r.counts.items()}}
-            for (a, b), c, r in zip(cuts, counts, rs)]
-    return lam[order], err[order], res2[order], vec[:, order], meta
+            for j, r in zip(mine, rs)]
+    return lam[order], err[order], res2[order], vec[:, order] if vec.size else vec, meta
 
 
 def run_record(job: Job, model, mixed: bool, block: int, lam, err, res2, meta) -> dict:
@@ -177,31 +228,63 @@ def run_record(job: Job, model, mixed: bool, block: int, lam, err, res2, meta) -
 
 
 def run(job: Job, mixed: bool = False, block: int | None = None, dry_run: bool = False, out=sys.stdout,
-        slices: int = 0) -> dict:
-    from .model import Model
+        slices: int = 0, group: Group | None = None) -> dict:
+    """One job.  Under torchrun every rank holds the whole operator on its
+    GPU and solves every size-th slice (at least one slice per rank); the
+    first rank prints, writes the node lists and the run record, and every
+    rank writes its own eigenvectors under their indices in the global
+    ascending order."""
+    from .model import Model, write_vector
+    grp = group or Group()
+    lead = grp.rank == 0
+    say = out if lead else io.StringIO()
     model = Model.load(job.base_path, job.porder, gravity=job.gravity)
     info = model.info()
-    print(f" JOB = {job.job}{'  (reference gravity)' if job.gravity else ''}", file=out)
-    print(f" mesh name: {job.basename}   polynomial order {job.porder}", file=out)
-    print(f" input directory: {job.inputdir}   output directory: {job.outputdir}", file=out)
-    print(f" lower / upper frequency in mHz {job.lowfreq} {job.upfreq}", file=out)
+    print(f" JOB = {job.job}{'  (reference gravity)' if job.gravity else ''}", file=say)
+    print(f" mesh name: {job.basename}   polynomial order {job.porder}", file=say)
+    print(f" input directory: {job.inputdir}   output directory: {job.outputdir}", file=say)
+    print(f" lower / upper frequency in mHz {job.lowfreq} {job.upfreq}", file=say)
     print(f" {info.ntet} tetrahedra ({info.n_fluid_tets} fluid), {info.n} displacement and {info.np} pressure DOFs",
-          file=out)
-    summary = {"ntet": info.ntet, "n": info.n, "np": info.np, "gravity": job.gravity}
+          file=say)
+    summary = {"ntet": info.ntet, "n": info.n, "np": info.np, "gravity": job.gravity, "ranks": grp.size}
     if dry_run:
         return summary
     if block is None:
         block = 32 if mixed else 0
-    with make_solver(model.operators(), job.porder, mixed) as sv:
-        lam, err, res2, vec, meta = _solve(sv, job, block, slices, out)
-    report(lam, err, out=out)
-    os.makedirs(job.outputdir or ".", exist_ok=True)
-    prefix = model.write_results(job.outputdir, job.basename, job.lowfreq, job.upfreq, vec, job=job.job, nproc=1)
+    if grp.size > 1:
+        slices = max(slices, grp.size)
+    with make_solver(model.operators(), job.porder, mixed, device=grp.local) as sv:
+        lam, err, res2, vec, meta = _solve(sv, job, block, slices, say, grp)
+    # global ascending order: the first rank ranks every eigenvalue, each
+    # rank learns the file indices of its own
+    parts = grp.gather((lam, err, res2, meta))
+    index = None
+    if lead:
+        L = np.concatenate([p[0] for p in parts])
+        order = np.argsort(L, kind="stable")
+        pos = np.empty(len(L), dtype=np.int64)
+        pos[order] = np.arange(len(L))
+        bounds = np.cumsum([0] + [len(p[0]) for p in parts])
+        index = [pos[bounds[r]:bounds[r + 1]].tolist() for r in range(grp.size)]
+        glam = L[order]
+        gerr = np.concatenate([p[1] for p in parts])[order]
+        gres2 = np.concatenate([p[2] for p in parts])[order]
+        gmeta = sorted((m for p in parts for m in p[3]), key=lambda m: m["slice"])
+        report(glam, gerr, out=out)
+        os.makedirs(job.outputdir or ".", exist_ok=True)
+        prefix = model.write_results(job.outputdir, job.basename, job.lowfreq, job.upfreq, np.zeros((info.n, 0)),
+                                     job=job.job, nproc=1)
+    prefix, index = grp.bcast((prefix, index) if lead else None)
+    for k, i in enumerate(index[grp.rank]):
+        write_vector(f"{prefix}_{i + 1}.dat", vec[:, k])
+    grp.gather(None)  # every rank's files are written
+    if not lead:
+        return dict(summary, nev_local=len(lam), prefix=prefix)
     print(" save eigenvectors: " + prefix + "_<i>.dat", file=out)
     with open(prefix + "_run.json", "w") as f:
-        json.dump(run_record(job, model, mixed, block, lam, err, res2, meta), f, indent=1)
+        json.dump(dict(run_record(job, model, mixed, block, glam, gerr, gres2, gmeta), ranks=grp.size), f, indent=1)
     print(" run record: " + prefix + "_run.json", file=out)
-    summary.update(nev=len(lam), prefix=prefix, lam=lam)
+    summary.update(nev=len(glam), prefix=prefix, lam=glam)
     return summary
 
 
@@ -219,7 +302,11 @@ def main(argv=None) -> int:
     except ConfError as e:
         print(e, file=sys.stderr)
         return 2
-    run(job, mixed=a.mixed, block=a.block, dry_run=a.dry_run, slices=a.slices)
+    grp = Group()
+    try:
+        run(job, mixed=a.mixed, block=a.block, dry_run=a.dry_run, slices=a.slices, group=grp)
+    finally:
+        grp.close()
     return 0
 
 

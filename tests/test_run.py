@@ -89,7 +89,7 @@ def test_dry_run(tmp_path, job):
 class _OracleSolver:
     """Stand-in for the GPU context: the oracle's solve, unscaled vectors."""
 
-    def __init__(self, mats, porder, mixed):
+    def __init__(self, mats, porder, mixed, device=0):
         from oracle import oracle as O
         self.O, self.op = O, O.setup_operator(mats, porder)
 
@@ -164,4 +164,57 @@ def test_sliced_job_matches_the_single_interval(tmp_path, monkeypatch):
     assert sliced["nev"] == whole["nev"]
     assert np.max(np.abs(sliced["lam"] - whole["lam"]) / whole["lam"]) < 1e-10
     assert np.all(np.diff(sliced["lam"]) >= 0)
+
+
+def _dist_rank(rank, ws, port, conf, q):
+    import sys as _sys
+    _sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws),
+                      LOCAL_RANK=str(rank))
+    from normalmodes_gb300 import run as RR
+    from tests.test_run import _OracleSolver as Stand
+    RR.make_solver = Stand
+    grp = RR.Group()
+    try:
+        s = RR.run(RR.read_global_conf(conf), out=io.StringIO(), slices=3, group=grp)
+        q.put((rank, {k: (v.tolist() if isinstance(v, np.ndarray) else v) for k, v in s.items()}))
+    finally:
+        grp.close()
+
+
+def test_slices_across_two_ranks(tmp_path, monkeypatch):
+    """torchrun form (one GPU per rank, operator replicated, slices shared
+    out, here two gloo ranks with the oracle standing in for the GPU): the
+    eigenvalues and eigenvector files are those of the single-rank job, each
+    vector written once under its global index."""
+    import torch.multiprocessing as mp
+    conf = _job_files(tmp_path, 2)
+    monkeypatch.setattr(R, "make_solver", _OracleSolver)
+    whole = R.run(R.read_global_conf(conf), out=io.StringIO())
+    ref_files = {i: np.fromfile(f"{whole['prefix']}_{i + 1}.dat") for i in range(whole["nev"])}
+    for i in range(whole["nev"]):
+        os.remove(f"{whole['prefix']}_{i + 1}.dat")
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29600 + os.getpid() % 1000
+    procs = [ctx.Process(target=_dist_rank, args=(r, 2, port, conf, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = dict(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    lead = out[0]
+    assert lead["ranks"] == 2 and lead["nev"] == whole["nev"]
+    assert out[0]["prefix"] == out[1]["prefix"] == whole["prefix"]
+    assert np.max(np.abs(np.array(lead["lam"]) - whole["lam"]) / whole["lam"]) < 1e-10
+    assert 0 < out[1]["nev_local"] < whole["nev"]
+    from normalmodes_gb300.model import Model
+    m = Model.load(R.read_global_conf(conf).base_path, 1, gravity=True)
+    A, B = m.csr("A").to_scipy(), m.csr("B").to_scipy()
+    for i in range(whole["nev"]):
+        x = np.fromfile(f"{whole['prefix']}_{i + 1}.dat")
+        assert x.size == ref_files[i].size
+        assert abs((x @ (A @ x)) / (x @ (B @ x)) / whole["lam"][i] - 1) < 1e-9
+    assert not os.path.exists(f"{whole['prefix']}_{whole['nev'] + 1}.dat")
 
