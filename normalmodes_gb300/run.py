@@ -25,6 +25,10 @@ with its configuration file and its result files, on this library.
 * ``--slices N`` cuts the interval into N slices of equal estimated
   eigenvalue count (nm_slice_spectrum) and solves them on one context
   (nm_solve_batched); the eigenpairs are merged in ascending order.
+* ``--checkpoint`` saves every solved slice (and the slice list) as
+  ``<prefix>_ckpt_slice<j>.npz``; ``--resume`` loads them instead of solving
+  those slices again, so an interrupted multi-slice job redoes only what is
+  missing.
 * ``--dry-run`` stops before the GPU: configuration, model, assembly.
 """
 from __future__ import annotations
@@ -173,21 +177,65 @@ class Group:
             self._own = False
 
 
-def _solve(sv, job: Job, block: int, slices: int, out, grp: Group):
+def _save_slice(path: str, r) -> None:
+    """Checkpoint of one solved slice (written to a temporary name first, so
+    an interrupted write leaves no checkpoint)."""
+    tmp = path + ".part.npz"
+    vec = r.vec if r.vec is not None else np.zeros((0, 0))
+    np.savez(tmp, lam=r.lam, err_ref=r.err_ref, res2=r.res2, vec=vec, xintv=np.asarray(r.xintv, dtype=np.float64),
+             pol_deg=int(r.pol_deg), lanczos_steps=int(r.lanczos_steps),
+             times=json.dumps({k: float(v) for k, v in r.times.items()}),
+             counts=json.dumps({k: int(v) for k, v in r.counts.items()}))
+    os.replace(tmp, path)
+
+
+def _load_slice(path: str):
+    from types import SimpleNamespace
+    with np.load(path) as z:
+        return SimpleNamespace(lam=z["lam"], err_ref=z["err_ref"], res2=z["res2"], vec=z["vec"],
+                               xintv=tuple(z["xintv"]), pol_deg=int(z["pol_deg"]),
+                               lanczos_steps=int(z["lanczos_steps"]), times=json.loads(str(z["times"])),
+                               counts=json.loads(str(z["counts"])))
+
+
+def _solve(sv, job: Job, block: int, slices: int, out, grp: Group, ckpt: str | None = None, resume: bool = False):
     """One interval (nm_solve), or `slices` slices of equal estimated
     eigenvalue count (nm_slice_spectrum, on the first rank) solved on this
     rank's context (nm_solve_batched): slice j belongs to rank j mod size.
+    With `ckpt` every solved slice (and the slice list) is saved under that
+    prefix; with `resume` saved slices are loaded instead of solved.
     Returns this rank's eigenpairs in ascending order and per-slice records."""
     if slices <= 1:
-        cuts, counts, mine = [(job.lowfreq, job.upfreq)], [None], [0]
-        rs = [sv.solve(job.lowfreq, job.upfreq, want_vectors=True, unscale=True, block=block)]
+        cuts, counts = [(job.lowfreq, job.upfreq)], [None]
     else:
-        cuts, counts = grp.bcast(sv.slice_spectrum(job.lowfreq, job.upfreq, slices) if grp.rank == 0 else None)
+        saved = ckpt + "_slices.json" if ckpt else None
+        if grp.rank == 0 and resume and saved and os.path.exists(saved):
+            cc = json.load(open(saved))
+            cc = ([tuple(c) for c in cc["cuts"]], cc["counts"])
+        elif grp.rank == 0:
+            cc = sv.slice_spectrum(job.lowfreq, job.upfreq, slices)
+            cc = ([tuple(map(float, c)) for c in cc[0]], [float(x) for x in cc[1]])
+            if saved:
+                json.dump({"cuts": cc[0], "counts": cc[1]}, open(saved, "w"))
+        cuts, counts = grp.bcast(cc if grp.rank == 0 else None)
         print(" spectrum slices (mHz) and estimated eigenvalue counts:", file=out)
         for j, ((a, b), c) in enumerate(zip(cuts, counts)):
             print(f"   {a:.9f} {b:.9f} {c:10.1f}   rank {j % grp.size}", file=out)
-        mine = [j for j in range(len(cuts)) if j % grp.size == grp.rank]
-        rs = sv.solve_batched([cuts[j] for j in mine], want_vectors=True, unscale=True, block=block) if mine else []
+    mine = [j for j in range(len(cuts)) if j % grp.size == grp.rank]
+    rs = []
+    for j in mine:
+        path = f"{ckpt}_slice{j}.npz" if ckpt else None
+        if resume and path and os.path.exists(path):
+            rs.append(_load_slice(path))
+            print(f" slice {j}: resumed from {path}", file=out)
+            continue
+        if len(cuts) == 1:
+            r = sv.solve(job.lowfreq, job.upfreq, want_vectors=True, unscale=True, block=block)
+        else:
+            r = sv.solve_batched([cuts[j]], want_vectors=True, unscale=True, block=block)[0]
+        if path:
+            _save_slice(path, r)
+        rs.append(r)
     if rs:
         lam = np.concatenate([r.lam for r in rs])
         err = np.concatenate([r.err_ref for r in rs])
@@ -228,7 +276,7 @@ def run_record(job: Job, model, mixed: bool, block: int, lam, err, res2, meta) -
 
 
 def run(job: Job, mixed: bool = False, block: int | None = None, dry_run: bool = False, out=sys.stdout,
-        slices: int = 0, group: Group | None = None) -> dict:
+        slices: int = 0, group: Group | None = None, checkpoint: bool = False, resume: bool = False) -> dict:
     """One job.  Under torchrun every rank holds the whole operator on its
     GPU and solves every size-th slice (at least one slice per rank); the
     first rank prints, writes the node lists and the run record, and every
@@ -253,8 +301,16 @@ def run(job: Job, mixed: bool = False, block: int | None = None, dry_run: bool =
         block = 32 if mixed else 0
     if grp.size > 1:
         slices = max(slices, grp.size)
+    # the result-file prefix (the first rank writes the node lists)
+    prefix = None
+    if lead:
+        os.makedirs(job.outputdir or ".", exist_ok=True)
+        prefix = model.write_results(job.outputdir, job.basename, job.lowfreq, job.upfreq, np.zeros((info.n, 0)),
+                                     job=job.job, nproc=1)
+    prefix = grp.bcast(prefix)
+    ckpt = prefix + "_ckpt" if (checkpoint or resume) else None
     with make_solver(model.operators(), job.porder, mixed, device=grp.local) as sv:
-        lam, err, res2, vec, meta = _solve(sv, job, block, slices, say, grp)
+        lam, err, res2, vec, meta = _solve(sv, job, block, slices, say, grp, ckpt, resume)
     # global ascending order: the first rank ranks every eigenvalue, each
     # rank learns the file indices of its own
     parts = grp.gather((lam, err, res2, meta))
@@ -271,10 +327,7 @@ def run(job: Job, mixed: bool = False, block: int | None = None, dry_run: bool =
         gres2 = np.concatenate([p[2] for p in parts])[order]
         gmeta = sorted((m for p in parts for m in p[3]), key=lambda m: m["slice"])
         report(glam, gerr, out=out)
-        os.makedirs(job.outputdir or ".", exist_ok=True)
-        prefix = model.write_results(job.outputdir, job.basename, job.lowfreq, job.upfreq, np.zeros((info.n, 0)),
-                                     job=job.job, nproc=1)
-    prefix, index = grp.bcast((prefix, index) if lead else None)
+    index = grp.bcast(index)
     for k, i in enumerate(index[grp.rank]):
         write_vector(f"{prefix}_{i + 1}.dat", vec[:, k])
     grp.gather(None)  # every rank's files are written
@@ -296,6 +349,8 @@ def main(argv=None) -> int:
     ap.add_argument("--dry-run", action="store_true", help="read, load and assemble only")
     ap.add_argument("--slices", type=int, default=0,
                     help="solve N slices of equal estimated eigenvalue count on one context")
+    ap.add_argument("--checkpoint", action="store_true", help="save every solved slice beside the results")
+    ap.add_argument("--resume", action="store_true", help="load the slices an earlier run saved")
     a = ap.parse_args(argv)
     try:
         job = read_global_conf(a.conf)
@@ -304,7 +359,8 @@ def main(argv=None) -> int:
         return 2
     grp = Group()
     try:
-        run(job, mixed=a.mixed, block=a.block, dry_run=a.dry_run, slices=a.slices, group=grp)
+        run(job, mixed=a.mixed, block=a.block, dry_run=a.dry_run, slices=a.slices, group=grp,
+            checkpoint=a.checkpoint, resume=a.resume)
     finally:
         grp.close()
     return 0

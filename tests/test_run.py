@@ -218,3 +218,32 @@ def test_slices_across_two_ranks(tmp_path, monkeypatch):
         assert abs((x @ (A @ x)) / (x @ (B @ x)) / whole["lam"][i] - 1) < 1e-9
     assert not os.path.exists(f"{whole['prefix']}_{whole['nev'] + 1}.dat")
 
+
+
+def test_checkpoint_and_resume(tmp_path, monkeypatch):
+    """--checkpoint saves the slice list and every solved slice; --resume
+    loads them and solves only the missing ones, with the same result."""
+    conf = _job_files(tmp_path, 2)
+    monkeypatch.setattr(R, "make_solver", _OracleSolver)
+    first = R.run(R.read_global_conf(conf), out=io.StringIO(), slices=3, checkpoint=True)
+    ck = first["prefix"] + "_ckpt"
+    assert os.path.exists(ck + "_slices.json")
+    assert all(os.path.exists(f"{ck}_slice{j}.npz") for j in range(3))
+    os.remove(f"{ck}_slice1.npz")
+    solved = []
+
+    class Counting(_OracleSolver):
+        def slice_spectrum(self, lo, hi, n):
+            raise AssertionError("the slice list must come from the checkpoint")
+
+        def solve_batched(self, cuts, want_vectors, unscale, block):
+            solved.extend(cuts)
+            return super().solve_batched(cuts, want_vectors, unscale, block)
+
+    monkeypatch.setattr(R, "make_solver", Counting)
+    out = io.StringIO()
+    again = R.run(R.read_global_conf(conf), out=out, slices=3, resume=True)
+    assert len(solved) == 1
+    assert out.getvalue().count("resumed from") == 2
+    assert again["nev"] == first["nev"]
+    assert np.array_equal(again["lam"], first["lam"])
