@@ -1,7 +1,9 @@
 """A NormalModes job on the GPU: the reference's driver (src/mainnm.f90)
 with its configuration file and its result files, on this library.
 
-    python -m normalmodes_gb300.run global_conf [--mixed] [--block 0|32] [--slices N] [--dry-run]
+    python -m normalmodes_gb300.run global_conf [--mixed] [--block 0|32] [--slices N]
+                                                [--checkpoint] [--resume] [--dry-run]
+    python -m torch.distributed.run --nproc-per-node G -m normalmodes_gb300.run global_conf --slices N
 
 * ``global_conf`` is read as the reference reads it (para_init,
   src/mod_para.f90:79-137, with string_conf of src/mod_string.f90): on each
@@ -25,6 +27,9 @@ with its configuration file and its result files, on this library.
 * ``--slices N`` cuts the interval into N slices of equal estimated
   eigenvalue count (nm_slice_spectrum) and solves them on one context
   (nm_solve_batched); the eigenpairs are merged in ascending order.
+* Under torchrun (one GPU per rank) every rank loads the operator and
+  solves every size-th slice; only the slices, eigenvalues and file indices
+  cross ranks (gloo), and the files are those of a one-GPU job.
 * ``--checkpoint`` saves every solved slice (and the slice list) as
   ``<prefix>_ckpt_slice<j>.npz``; ``--resume`` loads them instead of solving
   those slices again, so an interrupted multi-slice job redoes only what is
