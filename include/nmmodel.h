@@ -105,6 +105,14 @@ int nmm_load_gravity(nmm_model* m, const char* base_path);
  * reference's demo gravity files).  NMM_ERR_STATE for loaded models. */
 int nmm_ball_gravity(nmm_model* m, double G);
 
+/* Write the model in the reference's input files under base_path (the files
+ * nmm_load_files and nmm_load_gravity read): _mesh.header, _ele.dat,
+ * _node.dat, _neigh.dat (int32 Ntet x 4, the tetrahedron opposite each
+ * vertex, 1-based, -1 on the boundary), _{vp,vs,rho}_pod_<p>_true.dat and,
+ * when set, the gravity file.  Vertices are numbered by increasing node id
+ * among the vertex nodes (the model's own numbering for P1). */
+int nmm_write_model_files(const nmm_model* m, const char* base_path);
+
 /* The gravity field (borrowed, 3 pNp Ntet values) or NULL when off. */
 int nmm_get_gravity(const nmm_model* m, const double** g0);
 

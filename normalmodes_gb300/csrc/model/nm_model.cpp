@@ -1685,6 +1685,78 @@ int nmm_ball_gravity(nmm_model* m, double G) {
   return nmm_set_gravity(m, g0.data());
 }
 
+// The model in the reference's input files (the files nmm_load_files and
+// nmm_load_gravity read; src/mod_geometry.f90:83-425, src/mod_cg_models.f90:301-429):
+// vertices are numbered by increasing node id among the nodes at vertex
+// positions (for P1 models, the model's own numbering), tetrahedra keep
+// their order, the neighbour file lists the tetrahedron opposite each
+// vertex (1-based, -1 on the outer boundary) and the nodal material and
+// gravity keep the reference element's local order.
+int nmm_write_model_files(const nmm_model* m, const char* base) {
+  if (!m || !base) return fail(NMM_ERR_ARG, "null argument");
+  const std::string b(base), ps = std::to_string(m->porder);
+  const int p = m->pnp;
+  std::vector<int> vid(m->nnode, -1);
+  for (int k = 0; k < m->ntet; ++k)
+    for (int v = 0; v < 4; ++v) vid[m->tet[(size_t)p * k + m->ref.vord[v]]] = 0;
+  int nv = 0;
+  for (int i = 0; i < m->nnode; ++i)
+    if (vid[i] == 0) vid[i] = nv++;
+  std::vector<int> ele(4 * (size_t)m->ntet);
+  for (int k = 0; k < m->ntet; ++k)
+    for (int v = 0; v < 4; ++v) ele[4 * (size_t)k + v] = vid[m->tet[(size_t)p * k + m->ref.vord[v]]];
+  std::vector<double> xyz(3 * (size_t)nv);
+  for (int i = 0; i < m->nnode; ++i)
+    if (vid[i] >= 0)
+      for (int c = 0; c < 3; ++c) xyz[3 * (size_t)vid[i] + c] = m->xyz[3 * (size_t)i + c];
+  // neighbours across the face opposite each vertex
+  std::vector<std::pair<std::array<int, 3>, int>> faces((size_t)m->ntet * 4);
+  for (int k = 0; k < m->ntet; ++k)
+    for (int f = 0; f < 4; ++f) {
+      std::array<int, 3> a;
+      int q = 0;
+      for (int v = 0; v < 4; ++v)
+        if (v != f) a[q++] = ele[4 * (size_t)k + v];
+      std::sort(a.begin(), a.end());
+      faces[4 * (size_t)k + f] = {a, 4 * k + f};
+    }
+  std::sort(faces.begin(), faces.end());
+  std::vector<int> neigh(4 * (size_t)m->ntet, -1);
+  for (size_t i = 0; i < faces.size();) {
+    size_t j = i + 1;
+    while (j < faces.size() && faces[j].first == faces[i].first) ++j;
+    if (j - i > 2) return fail(NMM_ERR_MESH, "a face shared by more than two tetrahedra");
+    if (j - i == 2) {
+      neigh[faces[i].second] = faces[i + 1].second / 4 + 1;
+      neigh[faces[i + 1].second] = faces[i].second / 4 + 1;
+    }
+    i = j;
+  }
+  for (auto& e : ele) ++e;  // 1-based
+  auto put = [&](const std::string& path, const void* data, size_t bytes) -> int {
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) return fail(NMM_ERR_IO, "cannot open " + path);
+    const size_t w = bytes ? std::fwrite(data, 1, bytes, f) : 0;
+    std::fclose(f);
+    return w == bytes ? NMM_OK : fail(NMM_ERR_IO, "short write " + path);
+  };
+  const std::string hdr = std::to_string(m->ntet) + " " + std::to_string(nv);
+  const size_t nm = (size_t)p * m->ntet * sizeof(double);
+  int rc;
+  if ((rc = put(b + "_mesh.header", hdr.data(), hdr.size())) ||
+      (rc = put(b + "_ele.dat", ele.data(), ele.size() * sizeof(int))) ||
+      (rc = put(b + "_node.dat", xyz.data(), xyz.size() * sizeof(double))) ||
+      (rc = put(b + "_neigh.dat", neigh.data(), neigh.size() * sizeof(int))) ||
+      (rc = put(b + "_vp_pod_" + ps + "_true.dat", m->vp.data(), nm)) ||
+      (rc = put(b + "_vs_pod_" + ps + "_true.dat", m->vs.data(), nm)) ||
+      (rc = put(b + "_rho_pod_" + ps + "_true.dat", m->rho.data(), nm)))
+    return rc;
+  if (!m->g0.empty() &&
+      (rc = put(b + "_pod_" + ps + "_potential_acceleration_true.dat", m->g0.data(), m->g0.size() * sizeof(double))))
+    return rc;
+  return NMM_OK;
+}
+
 int nmm_get_gravity(const nmm_model* m, const double** g0) {
   if (!m || !g0) return fail(NMM_ERR_ARG, "null argument");
   *g0 = m->g0.empty() ? nullptr : m->g0.data();

@@ -81,6 +81,7 @@ def lib() -> C.CDLL:
         L.nmm_load_gravity.argtypes = [vp, C.c_char_p]
         L.nmm_ball_gravity.argtypes = [vp, C.c_double]
         L.nmm_get_gravity.argtypes = [vp, C.POINTER(C.POINTER(C.c_double))]
+        L.nmm_write_model_files.argtypes = [vp, C.c_char_p]
         L.nmm_write_vector.argtypes = [C.c_char_p, C.POINTER(C.c_double), C.c_longlong]
         L.nmm_last_error.restype = C.c_char_p
         L.nmm_destroy.argtypes = [vp]
@@ -170,6 +171,11 @@ class Model:
         _check(lib().nmm_ball_gravity(self._h, G))
         if assemble:
             self.assemble()
+
+    def write_model_files(self, base_path: str) -> None:
+        """The model in the reference's input files (nmm_write_model_files):
+        Model.load(base_path, p, gravity=...) reads it back."""
+        _check(lib().nmm_write_model_files(self._h, base_path.encode()))
 
     def gravity(self):
         """The reference gravity (ntet x pnp x 3, m/s^2), or None (JOB = 1)."""
