@@ -93,3 +93,49 @@ def test_refinement_recurrence():
     direct = _cheb_matrix_poly(L, coefs) @ Bu - _cheb_scalar(lt, deg) * Bu
     assert np.allclose(Dk, direct, rtol=1e-9, atol=1e-9 * np.abs(direct).max())
     assert np.isclose(tk, _cheb_scalar(lt, deg))
+
+
+def test_range_form_keeps_the_null_space_exact_in_fp32():
+    """Why the mixed path filters in range form: with the recurrence run in
+    FP32, the plain form leaves FP32 rounding in the null space of A (the
+    zero-frequency fluid modes), which the Lanczos then has to carry; the
+    range form p(0) Z + A B^-1 Y, with Y in FP32 and only the last product
+    by A in FP64, has exactly p(0) times Z's null-space content, to FP64
+    rounding."""
+    A, B = _pencil(n=60, seed=7)
+    n = A.shape[0]
+    Binv = np.linalg.inv(B)
+    cc, dd, deg = 1.0, 1.05, 30
+    mu = np.random.default_rng(3).standard_normal(deg + 1) / (1 + np.arange(deg + 1))
+    Z = np.random.default_rng(4).standard_normal((n, 3))
+    L = (A @ Binv - cc * np.eye(n)) / dd
+    f32 = np.float32
+    L32 = L.astype(f32)
+    # plain form, FP32 recurrence
+    Tkm1, Tk = Z.astype(f32), (L32 @ Z.astype(f32))
+    acc = (f32(mu[0]) * Tkm1 + f32(mu[1]) * Tk)
+    for k in range(2, deg + 1):
+        Tkm1, Tk = Tk, f32(2) * (L32 @ Tk) - Tkm1
+        acc = acc + f32(mu[k]) * Tk
+    W_plain = acc.astype(np.float64)
+    # range form, FP32 recurrence for Y, final A B^-1 in FP64
+    l0 = -cc / dd
+    tau = [_cheb_scalar(l0, k) for k in range(deg + 1)]
+    p0 = sum(mu[k] * tau[k] for k in range(deg + 1))
+    Z32 = Z.astype(f32)
+    Ekm1, Ek = np.zeros_like(Z32), Z32 / f32(dd)
+    Y = f32(mu[1]) * Ek
+    for k in range(1, deg):
+        Ekp1 = f32(2) * (L32 @ Ek) - Ekm1 + f32(2 * tau[k] / dd) * Z32
+        Y = Y + f32(mu[k + 1]) * Ekp1
+        Ekm1, Ek = Ek, Ekp1
+    W_range = p0 * Z + A @ (Binv @ Y.astype(np.float64))
+    w, V = np.linalg.eigh(A)
+    N = V[:, :5]
+    exact = p0 * (N.T @ Z)
+    scale = np.abs(W_range).max()
+    err_plain = np.abs(N.T @ W_plain - exact).max() / scale
+    err_range = np.abs(N.T @ W_range - exact).max() / scale
+    assert err_plain > 1e-9          # FP32 rounding lands in the null space
+    assert err_range < 1e-13         # the range form keeps it at FP64 level
+    assert err_plain > 1e4 * err_range
