@@ -30,6 +30,9 @@ with its configuration file and its result files, on this library.
 * Under torchrun (one GPU per rank) every rank loads the operator and
   solves every size-th slice; only the slices, eigenvalues and file indices
   cross ranks (gloo), and the files are those of a one-GPU job.
+* The first rank also writes the reference's run log,
+  ``<outputdir><basename>_0.log`` (numbered phases and elapsed times,
+  src/mod_utility.f90:39-148).
 * ``--checkpoint`` saves every solved slice (and the slice list) as
   ``<prefix>_ckpt_slice<j>.npz``; ``--resume`` loads them instead of solving
   those slices again, so an interrupted multi-slice job redoes only what is
@@ -44,6 +47,7 @@ import json
 import math
 import os
 import sys
+import time
 from dataclasses import dataclass
 
 import numpy as np
@@ -112,6 +116,37 @@ def read_global_conf(path: str) -> Job:
     if lo >= hi:
         raise ConfError("Error: please check input frequencies")
     return Job(job, v["basename"], v["inputdir"], v["outputdir"], lo, hi, porder)
+
+
+class PhaseLog:
+    """The reference's run log, <outputdir><basename>_0.log (openlogfile,
+    writelog and report_time, src/mod_utility.f90:39-148): numbered phase
+    messages and the wall time elapsed since the start.  The suffix is 0
+    as in the reference, whose name takes the rank of process 0."""
+
+    def __init__(self, job: "Job", enabled: bool):
+        self.f = None
+        self.n = 0
+        self.t0 = time.perf_counter()
+        if enabled:
+            os.makedirs(job.outputdir or ".", exist_ok=True)
+            self.f = open(f"{job.outputdir}{job.basename}_0.log", "w")
+            self.f.write("  Start program at time elapsed = 0.0 second.\n")
+
+    def phase(self, msg: str) -> None:
+        if self.f:
+            self.n += 1
+            self.f.write(f"{self.n:4d}. {msg}\n")
+
+    def stamp(self) -> None:
+        if self.f:
+            self.f.write(f"  Time elapsed = {time.perf_counter() - self.t0:24.15f}      seconds.\n")
+            self.f.flush()
+
+    def close(self) -> None:
+        if self.f:
+            self.f.close()
+            self.f = None
 
 
 # the default-real PI literal of src/mod_pevsl.f90, widened to double
@@ -287,11 +322,25 @@ def run(job: Job, mixed: bool = False, block: int | None = None, dry_run: bool =
     first rank prints, writes the node lists and the run record, and every
     rank writes its own eigenvectors under their indices in the global
     ascending order."""
-    from .model import Model, write_vector
     grp = group or Group()
     lead = grp.rank == 0
     say = out if lead else io.StringIO()
-    model = Model.load(job.base_path, job.porder, gravity=job.gravity)
+    log = PhaseLog(job, lead and not dry_run)
+    try:
+        return _run(job, mixed, block, dry_run, out, say, slices, grp, lead, checkpoint, resume, log)
+    finally:
+        log.close()
+
+
+def _run(job, mixed, block, dry_run, out, say, slices, grp, lead, checkpoint, resume, log) -> dict:
+    from .model import Model, write_vector
+    log.phase("Starting main program")
+    log.phase("Loading the mesh and models")
+    model = Model.load(job.base_path, job.porder, gravity=job.gravity, assemble=False)
+    log.stamp()
+    log.phase("Creating matrix")
+    model.assemble()
+    log.stamp()
     info = model.info()
     print(f" JOB = {job.job}{'  (reference gravity)' if job.gravity else ''}", file=say)
     print(f" mesh name: {job.basename}   polynomial order {job.porder}", file=say)
@@ -314,8 +363,12 @@ def run(job: Job, mixed: bool = False, block: int | None = None, dry_run: bool =
                                      job=job.job, nproc=1)
     prefix = grp.bcast(prefix)
     ckpt = prefix + "_ckpt" if (checkpoint or resume) else None
+    log.phase("Setting up the GPU operators")
     with make_solver(model.operators(), job.porder, mixed, device=grp.local) as sv:
+        log.stamp()
+        log.phase("solve the eigenvalue problem")
         lam, err, res2, vec, meta = _solve(sv, job, block, slices, say, grp, ckpt, resume)
+        log.stamp()
     # global ascending order: the first rank ranks every eigenvalue, each
     # rank learns the file indices of its own
     parts = grp.gather((lam, err, res2, meta))
@@ -333,6 +386,7 @@ def run(job: Job, mixed: bool = False, block: int | None = None, dry_run: bool =
         gmeta = sorted((m for p in parts for m in p[3]), key=lambda m: m["slice"])
         report(glam, gerr, out=out)
     index = grp.bcast(index)
+    log.phase("save eigenvectors")
     for k, i in enumerate(index[grp.rank]):
         write_vector(f"{prefix}_{i + 1}.dat", vec[:, k])
     grp.gather(None)  # every rank's files are written
@@ -342,6 +396,9 @@ def run(job: Job, mixed: bool = False, block: int | None = None, dry_run: bool =
     with open(prefix + "_run.json", "w") as f:
         json.dump(dict(run_record(job, model, mixed, block, glam, gerr, gres2, gmeta), ranks=grp.size), f, indent=1)
     print(" run record: " + prefix + "_run.json", file=out)
+    log.stamp()
+    log.phase("finalize everything")
+    log.stamp()
     summary.update(nev=len(glam), prefix=prefix, lam=glam)
     return summary
 

@@ -150,6 +150,13 @@ def test_whole_job_with_a_stand_in_solver(tmp_path, monkeypatch):
     assert np.allclose(rec["eigenpairs"]["lambda"], s["lam"]) and np.allclose(rec["eigenpairs"]["f_mhz"], f)
     sl = rec["solver"]["slices"]
     assert len(sl) == 1 and sl[0]["nev"] == s["nev"] and sl[0]["filter_degree"] > 0
+    # the reference's run log (src/mod_utility.f90:39-148)
+    log = open(str(tmp_path / "output" / "ball.1_0.log")).read().splitlines()
+    assert log[0] == "  Start program at time elapsed = 0.0 second."
+    assert log[1] == "   1. Starting main program"
+    phases = [ln[6:] for ln in log if ln[:4].strip().isdigit() and ln[4:6] == ". "]
+    assert phases[-3:] == ["solve the eigenvalue problem", "save eigenvectors", "finalize everything"]
+    assert sum("Time elapsed" in ln for ln in log) >= 5
 
 
 def test_sliced_job_matches_the_single_interval(tmp_path, monkeypatch):
