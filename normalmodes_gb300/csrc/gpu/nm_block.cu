@@ -1032,7 +1032,6 @@ void blk_ap_cheb_persistent(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b
   XT* d1 = work + 2 * len;
   XT* xi = work + 3 * len;
   blocks = std::max(1, std::min(blocks, (np + kRowsP - 1) / kRowsP));
-  cudaMemsetAsync(bar, 0, sizeof(GridBar), s);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks);
   cfg.blockDim = dim3(kTP);
@@ -1044,8 +1043,17 @@ void blk_ap_cheb_persistent(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b
   cfg.numAttrs = 1;
   const XT it = (XT)ch.inv_theta;
   int deg = ch.deg;
-  cudaLaunchKernelEx(&cfg, k_ap_cheb<VT, XT>, np, (const int*)Ap.rp, (const int*)Ap.ci, (const VT*)Ap.v, b, x, r, xi,
-                     d0, d1, (const double*)ch.d_coef, deg, it, bar, status);
+  cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), s);
+  if (e == cudaSuccess)
+    e = cudaLaunchKernelEx(&cfg, k_ap_cheb<VT, XT>, np, (const int*)Ap.rp, (const int*)Ap.ci, (const VT*)Ap.v, b, x,
+                           r, xi, d0, d1, (const double*)ch.d_coef, deg, it, bar, status);
+  if (e != cudaSuccess) {
+    // refused cooperative launch (not sticky): clear it and run the gather
+    // form of the same solve, which needs no co-resident CTAs
+    cudaGetLastError();
+    blk_ap_cheb<VT, XT>(Ap, ch, b, x, work, s);
+    return;
+  }
   nmg::add_launches(1);
 }
 

@@ -461,7 +461,6 @@ void cheb_solve_persistent(const Sell<VT>& M, const ChebSetup& ch, const XT* b, 
   int deg = ch.deg;
   blocks = std::min(blocks, nblk(n, kThreadsP));
   if (blocks < 1) blocks = 1;
-  cudaMemsetAsync(bar, 0, sizeof(GridBar), s);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks);
   cfg.blockDim = dim3(kThreadsP);
@@ -472,7 +471,18 @@ void cheb_solve_persistent(const Sell<VT>& M, const ChebSetup& ch, const XT* b, 
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k_cheb_persist<VT, XT>, v, b, x, r, xi, d0, d1, coef, deg, it, bar, status);
+  cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), s);
+  if (e == cudaSuccess)
+    e = cudaLaunchKernelEx(&cfg, k_cheb_persist<VT, XT>, v, b, x, r, xi, d0, d1, coef, deg, it, bar, status);
+  if (e != cudaSuccess) {
+    // A refused cooperative launch (more CTAs than can be co-resident, e.g.
+    // under MPS or a partitioned GPU) is not sticky and would leave x
+    // unwritten: clear it and run the same solve as separate launches, which
+    // need no co-residency.  A sticky error resurfaces at the next launch.
+    cudaGetLastError();
+    cheb_solve<VT, XT>(M, ch, b, x, work, s);
+    return;
+  }
   NM_COUNT(1);
 }
 // Test hook for the bounded wait: one block waits at the grid barrier for

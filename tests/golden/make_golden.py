@@ -32,18 +32,33 @@ SPECS = {
     "solid_p1_grav": dict(model=dict(n_cells=6, porder=1, fluid_core=0, gravity=True), porder=1,
                           interval=(0.1, 1.0), dense=True),
     "fs_p1_grav": dict(model=dict(n_cells=8, porder=1, gravity=True), porder=1, interval=(0.2, 1.0), dense=True),
+    # the layered P1 ball of about 10k tetrahedra (jittered) and 0.2-1.0 mHz
+    "ball12_p1": dict(model=dict(n_cells=12, porder=1), porder=1, interval=(0.2, 1.0), dense=False),
+    # the reference's own demo meshes (P1 inputs copied by make_ref_inputs.py),
+    # at the demo global_conf's interval 0.2-2.0 mHz
+    "const3k_p1": dict(files="CONST3k/CONST_1L_3k.1", porder=1, interval=(0.2, 2.0), dense=True),
+    "prem3k_p1": dict(files="PREM3k/prem_3L_3k.1", porder=1, interval=(0.2, 2.0), dense=True),
 }
+REF_INPUTS = os.path.join(HERE, "ref_inputs")
+
+
+def load_model(name: str) -> Model:
+    """The model of fixture `name`: a seeded ball, or reference input files."""
+    s = SPECS[name]
+    if "files" in s:
+        return Model.load(os.path.join(REF_INPUTS, s["files"]), s["porder"])
+    return Model.ball(**s["model"])
 
 
 def make(name: str) -> str:
     s = SPECS[name]
     t0 = time.time()
-    m = Model.ball(**s["model"])
+    m = load_model(name)
     mats = m.operators()
     op = O.setup_operator(mats, s["porder"])
     r = O.apply_pevsl(op, *s["interval"])
     out = dict(
-        model_kw=repr(s["model"]), porder=s["porder"], interval=np.array(s["interval"]),
+        model_kw=repr(s.get("model", s.get("files"))), porder=s["porder"], interval=np.array(s["interval"]),
         b_bounds=np.array(op.bounds["B"]), ap_bounds=np.array(op.bounds.get("Ap", (0.0, 0.0))),
         xintv=np.array(r.xintv, dtype=np.float64), pol_deg=r.pol.deg, pol_bar=r.pol.bar, pol_gam=r.pol.gam,
         lam=r.lam, err_ref=r.err_ref, res2=r.res2, steps=r.steps, n=op.n, np=op.np,

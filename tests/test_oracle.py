@@ -14,7 +14,7 @@ def _golden(name):
     return np.load(os.path.join(HERE, "golden", f"{name}.npz"))
 
 
-@pytest.mark.parametrize("name", ["solid_p1", "fs_p1", "solid_p1_grav", "fs_p1_grav"])
+@pytest.mark.parametrize("name", ["solid_p1", "fs_p1", "solid_p1_grav", "fs_p1_grav", "const3k_p1", "prem3k_p1"])
 def test_golden_fixtures_match_dense_solves(name):
     """The oracle's filtered-Lanczos eigenvalues (the fixtures the GPU tests
     compare with) against scipy.linalg.eigh of the same pencil."""

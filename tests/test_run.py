@@ -12,7 +12,10 @@ import pytest
 
 from normalmodes_gb300 import run as R
 
-REF_DEMO = os.environ.get("NM_REFERENCE_DEMOS", "/root/reference/demos/models/input")
+# committed copies of the reference's CONST3k / PREM3k P1 inputs and demo
+# global_conf (tests/golden/make_ref_inputs.py)
+REF_DEMO = os.environ.get("NM_REFERENCE_DEMOS",
+                          os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_inputs"))
 
 
 def _write_conf(path, **kv):
@@ -24,8 +27,9 @@ def _write_conf(path, **kv):
 
 
 def test_reference_demo_configurations():
-    demos = os.path.dirname(os.path.dirname(REF_DEMO))
-    conf = os.path.join(demos, "global_conf")
+    conf = os.path.join(REF_DEMO, "global_conf")
+    if not os.path.exists(conf):  # a full demos/models/input checkout keeps it two levels up
+        conf = os.path.join(os.path.dirname(os.path.dirname(REF_DEMO)), "global_conf")
     if not os.path.exists(conf):
         pytest.skip("reference demos not present")
     j = R.read_global_conf(conf)
