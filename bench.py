@@ -12,17 +12,25 @@ in 0.1-2.0 mHz.  "ball36-p2" is the same ball without the perturbation,
 "ball12-p1" the small P1 ball (10,368 tetrahedra, 0.2-1.0 mHz) that the CPU
 runs whole.
 
-A step is one end-to-end call of the public C-ABI on one spectrum slice:
-nm_create from pinned host CSR arrays (host-to-device copies inside),
-nm_solve (bounds, filter design, filtered Lanczos, Ritz vectors, residual
-check, eigenvectors back to the host), nm_destroy.
-  value : eigenpairs / time of the nm_solve part, timed with CUDA events on
-          the context's stream (operators resident in HBM when it starts);
-  e2e   : eigenpairs / wall time of the whole step.
-Warm-up steps are truncated solves (three block steps, maxit = 96) on a
-context created once, so they run every kernel of the timed step.  Every
-operator and block vector is larger than L2 (Ad alone is 1.2 GB), so no L2
-flush is needed between timed iterations.
+One bench run is ONE complete solve of the workload through the public
+C-ABI, timed as K contiguous steps (the driver's --steps K): the solve's
+block-Lanczos steps (one 32-vector filter application + Gram-Schmidt each)
+are cut into K equal groups; step 1 also holds nm_create from pinned host
+CSR arrays (host-to-device copies) and the bounds, step K the Ritz vectors,
+the FP64 refinement, the residual check and the eigenvectors' copy back to
+the host.  The K steps together are the whole job, timed between a
+barrier + synchronize on both sides, so
+  value : eigenpairs that pass the residual gate (err_ref <= 1e-10, the
+          reference's norm, src/mod_pevsl.f90:158) / time of nm_solve,
+          timed with CUDA events on the context's stream (operators resident
+          in HBM when it starts: the reference's timed region
+          src/mainnm.f90:43-44 to src/mod_pevsl.f90:203-204);
+  e2e   : the same eigenpairs / wall time of all K steps (create, solve,
+          vectors to the host, destroy).
+W warm-up steps are W block steps of a truncated solve on a context created
+once (bounds, filter graph, Gram-Schmidt, Rayleigh-Ritz, refinement and
+residual kernels all run).  Every operator and block vector is larger than
+L2 (Ad alone is 1.2 GB), so no L2 flush is needed between steps.
 
 `--impl reference` times the CPU path of the same workload (the FP64
 C/OpenMP restatement under oracle/ on all host cores, since the
@@ -69,8 +77,8 @@ REF_COUNTS = {"ball36-p2-lateral": dict(nev=1232, lanczos_steps=4401, degree=125
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--block", type=int, default=32)
@@ -269,6 +277,17 @@ def cpu_sample(name: str, op, seconds: float, t_setup: float = 0.0):
             "sample": sample, "t_degree_step_s": t_deg, "t_setup_s": t_setup}
 
 
+def step_cuts(t0: float, t_end: float, block_times: list, k: int) -> list:
+    """K + 1 boundaries of the K steps of one solve: t0, the end of every
+    (len / K)-th block-Lanczos step, t_end.  Step 1 thus also holds the set-up
+    before the first block step and step K everything after the last cut.
+    With fewer block steps than K the span is cut evenly."""
+    nb = len(block_times)
+    if nb < k:
+        return [t0 + (t_end - t0) * i / k for i in range(k + 1)]
+    return [t0] + [block_times[(i + 1) * nb // k - 1] for i in range(k - 1)] + [t_end]
+
+
 # ----------------------------------------------------------------------------- main
 def main():
     a = parse()
@@ -304,55 +323,65 @@ def main():
 
     import numpy as np
     import torch
-    from normalmodes_gb300.nmgpu import Solver, NM_PREC_MIXED, NM_PREC_FP64
+    from normalmodes_gb300.nmgpu import NM_PHASE_LANCZOS, NM_PREC_FP64, NM_PREC_MIXED, Solver
     prec = NM_PREC_MIXED if a.precision == "mixed" else NM_PREC_FP64
     dev = local
     torch.cuda.set_device(dev)
+    K = max(1, a.steps)
 
-    # pinned host copies of the operators: the inputs of every step
+    # pinned host copies of the operators: the inputs of the timed solve
     pinned = {}
     for k, m in mats.items():
         pinned[k] = type(m)(torch.from_numpy(m.rowptr).pin_memory().numpy(),
                             torch.from_numpy(m.col).pin_memory().numpy(),
                             torch.from_numpy(m.val).pin_memory().numpy(), m.shape)
 
-    # warm-up: truncated solves on one context
+    # warm-up: W block steps of a truncated solve on one context (kept for
+    # the kernel timings below)
     warm = Solver(pinned, wl["porder"], device=dev, precision=prec)
-    for _ in range(a.warmup):
-        warm.solve(lo, hi, block=a.block, maxit=3 * max(a.block, 32), want_vectors=True, unscale=True,
-                   allow_noconv=True)
+    W = max(a.warmup, 1)
+    warm.solve(lo, hi, block=a.block, maxit=W * max(a.block, 1), want_vectors=True, unscale=True,
+               allow_noconv=True)
     torch.cuda.synchronize()
 
-    nev_tot, kernels, t_solve, h2d, d2h = 0, 0, 0.0, 0, 0
-    res = None
+    # the timed job: one complete solve, cut into K steps at block boundaries
+    marks = []  # (phase, done, host time) at the solve's synchronised boundaries
+
+    def on_progress(phase, done, total):
+        marks.append((phase, done, time.perf_counter()))
+
     barrier(ws)
     torch.cuda.synchronize()
     with Clocks(dev) as clk:
         t0 = time.perf_counter()
-        for _ in range(a.steps):
-            sv = Solver(pinned, wl["porder"], device=dev, precision=prec)
-            h2d += sv.info().h2d_bytes
-            stream = torch.cuda.ExternalStream(sv.stream)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            res = sv.solve(lo, hi, block=a.block, want_vectors=True, unscale=True)
-            e1.record(stream)
-            e1.synchronize()
-            t_solve += e0.elapsed_time(e1) / 1e3
-            nev_tot += len(res.lam)
-            kernels += res.counts["kernels"]
-            d2h += 8 * (res.vec.size if res.vec is not None else 0) + 8 * 3 * len(res.lam)
-            sv.close()
+        sv = Solver(pinned, wl["porder"], device=dev, precision=prec)
+        h2d = sv.info().h2d_bytes
+        stream = torch.cuda.ExternalStream(sv.stream)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        res = sv.solve(lo, hi, block=a.block, want_vectors=True, unscale=True, progress=on_progress)
+        e1.record(stream)
+        e1.synchronize()
+        t_solve = e0.elapsed_time(e1) / 1e3
+        sv.close()
         torch.cuda.synchronize()
-        t_e2e = time.perf_counter() - t0
+        t_end = time.perf_counter()
     barrier(ws)
+    t_e2e = t_end - t0
     clocks = clk.summary()
-    value, value_e2e, t, te = aggregate(t_solve, t_e2e, nev_tot, ws)
+    gate = 1e-10
+    ok = res.err_ref <= gate
+    nev_ok = int(ok.sum())
+    value, value_e2e, t, te = aggregate(t_solve, t_e2e, nev_ok, ws)
+    d2h = 8 * (res.vec.size if res.vec is not None else 0) + 8 * 3 * len(res.lam)
+
+    cuts = step_cuts(t0, t_end, [tm for ph, _, tm in marks if ph == NM_PHASE_LANCZOS], K)
+    steps_ms = [round(1e3 * (cuts[k + 1] - cuts[k]), 1) for k in range(K)]
 
     # roofline of the dominant kernel: the block mass Chebyshev step
-    # (k_mass_cheb, 45 launches per B~^-1 apply), timed live with CUDA events
-    # on the context's stream
+    # (k_mass_cheb, one launch per inner Chebyshev degree), timed live with
+    # CUDA events on the context's stream
     which = 4 if a.block > 1 else 2
     ms, by, la = warm.time_op(which, 10)
     per_launch_ms = ms / la
@@ -386,30 +415,39 @@ def main():
     warm.close()
     if rank != 0:
         return
+    nev = len(res.lam)
     line = {
-        "metric": METRIC, "value": value, "unit": "eigenpairs/s", "n_gpus": ws, "steps": a.steps,
-        "warmup": a.warmup, "ms_per_step": t * 1e3 / a.steps, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": value, "unit": "eigenpairs/s", "n_gpus": ws, "steps": K,
+        "warmup": a.warmup, "ms_per_step": t * 1e3 / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 filter SpMM / f64 Lanczos, Rayleigh-Ritz" if prec == NM_PREC_MIXED else "f64",
+        "dtype": "f32 filter SpMM / f64 Lanczos, Rayleigh-Ritz, refinement residuals" if prec == NM_PREC_MIXED
+        else "f64",
         "data": "synthetic",
         "config": {"workload": wl["desc"], "n_dof": info.n, "n_pressure": info.np, "nnz": list(info.nnz),
                    "interval_mhz": [lo, hi], "precision": a.precision, "block": a.block,
+                   "step": f"1/{K} of one complete solve (block-Lanczos steps cut into {K} equal groups; "
+                           "create + bounds in the first, Ritz + refinement + residual check + copy-out in the last)",
                    "l2": "operators and block vectors exceed L2 (Ad 1.2 GB); no flush",
-                   "warmup_steps": "truncated solves (maxit 96)",
-                   "eigenpairs_per_step": len(res.lam), "lanczos_vectors": res.lanczos_steps,
-                   "filter_degree": res.pol_deg,
-                   "max_err_ref": float(res.err_ref.max()) if len(res.lam) else None,
-                   "median_err_ref": float(np.median(res.err_ref)) if len(res.lam) else None,
-                   "max_res2": float(res.res2.max()) if len(res.lam) else None,
+                   "warmup_steps": f"{W} block steps of a truncated solve",
+                   "residual_gate": f"err_ref <= {gate:g} (src/mod_pevsl.f90:158 RMS norm); value counts only those",
+                   "eigenpairs_found": nev, "eigenpairs_gated": nev_ok,
+                   "lanczos_vectors": res.lanczos_steps, "filter_degree": res.pol_deg,
+                   "max_err_ref": float(res.err_ref.max()) if nev else None,
+                   "median_err_ref": float(np.median(res.err_ref)) if nev else None,
+                   "max_res2": float(res.res2.max()) if nev else None,
+                   "median_res2": float(np.median(res.res2)) if nev else None,
+                   "refinement": {k: res.counts[k] for k in ("refine_passes", "refine_blocks", "refine_maxdeg",
+                                                             "refine_steps", "res2_before_refine")},
                    "parallelism": f"replicas x{ws}", "autotuned_gathers": tuned},
-        "gpu_launches": kernels,
+        "gpu_launches": res.counts["kernels"],
         "clocks": clocks,
         "roofline": roof,
         "spmv": spmv,
-        "e2e": {"value": value_e2e, "unit": "eigenpairs/s", "h2d_bytes_per_step": h2d // a.steps,
-                "d2h_bytes_per_step": d2h // a.steps},
+        "e2e": {"value": value_e2e, "unit": "eigenpairs/s", "h2d_bytes_per_step": h2d // K,
+                "d2h_bytes_per_step": d2h // K, "seconds": te},
+        "steps_ms": steps_ms,
         "cpu_baseline": cpu,
-        "times_s": res.times,
+        "times_s": {**res.times, "solve_events": t_solve},
     }
     print(json.dumps(line))
 

@@ -65,6 +65,18 @@ typedef struct {
 #define NM_PREC_FP64 0
 #define NM_PREC_MIXED 1
 
+/* Progress of nm_solve: called on the calling thread with the context's
+ * stream synchronised, at the end of each phase and after every Lanczos step
+ * (single vector) or block step (block path) and every refined block of Ritz
+ * vectors; `done` of `total` units of the phase (total -1 when open-ended).
+ * The reference prints the same milestones (src/mod_pevsl.f90:84-134). */
+typedef void (*nm_progress_fn)(void* data, int phase, int done, int total);
+#define NM_PHASE_BOUNDS 0  /* bounds of B^-1 A (LANBOUNDS) known                */
+#define NM_PHASE_LANCZOS 1 /* one more Lanczos step / block step; total = MAXIT */
+#define NM_PHASE_RITZ 2    /* Ritz vectors formed (first Rayleigh-Ritz done)     */
+#define NM_PHASE_REFINE 3  /* one more block of Ritz vectors refined / checked  */
+#define NM_PHASE_DONE 4    /* residual check done, results copied                */
+
 typedef struct {
   int maxit;          /* 0: 3*max(4*802,2000) = 9624 (src/mod_pevsl.f90:116-119) */
   double tol;         /* 0: 1e-5 (src/mod_pevsl.f90:52)                            */
@@ -78,9 +90,18 @@ typedef struct {
   int use_graph;      /* capture the filter in a CUDA graph (default on)           */
   int block;          /* 0/1: single-vector ChebLanNr (the reference's algorithm);
                          32: block filtered Lanczos, 32 vectors per filter pass  */
-  int polish;         /* mixed block path: degree of the FP64-accurate refinement
-                         of the Ritz vectors (0: 80, <0: off; capped at
-                         2 sqrt(lmax / (b - a)) for narrow spectra)             */
+  int polish;         /* mixed block path, refinement of the Ritz vectors towards
+                         FP64 residuals: 0 adaptive (degree per block of 32 Ritz
+                         vectors from their measured FP64 residuals, until
+                         err_ref <= resid_tol); > 0 a fixed plan of that degree
+                         for the lowest block (capped at 2 sqrt(lmax / (b - a)));
+                         < 0 off                                               */
+  double resid_tol;   /* adaptive refinement target for err_ref (0: 1e-10)        */
+  int refine_sweeps;  /* adaptive refinement: at most this many passes, each
+                         closed by an FP64 Rayleigh-Ritz (0: 2)                 */
+  int refine_maxdeg;  /* adaptive refinement: degree cap per block (0: 4000)      */
+  nm_progress_fn progress; /* host callback at phase boundaries (NULL: none)      */
+  void* progress_data;     /* first argument of progress                          */
 } nm_solve_opts;
 
 typedef struct {
@@ -101,6 +122,12 @@ typedef struct {
   double t_filter;       /* block path: seconds in the filter applications (CUDA events) */
   double t_orth;         /* block path: seconds in the block Gram-Schmidt (CUDA events)  */
   double t_eig;          /* block path: seconds in the projected (block-tridiagonal) eigensolves */
+  int refine_passes;     /* mixed block path, adaptive refinement: passes run (each
+                            closed by an FP64 Rayleigh-Ritz)                        */
+  int refine_blocks;     /* blocks of 32 Ritz vectors refined, over all passes      */
+  int refine_maxdeg;     /* largest refinement degree                               */
+  long long refine_steps;      /* block degree steps spent refining                 */
+  double res2_before_refine;   /* largest res2 of the Ritz vectors before refining  */
 } nm_result;
 
 typedef struct nm_ctx nm_ctx;

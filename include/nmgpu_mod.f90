@@ -13,6 +13,9 @@ module nmgpu_mod
   integer(c_int), parameter :: NM_OK = 0, NM_ERR_ARG = -1, NM_ERR_CUDA = -2, NM_ERR_OOM = -3, &
                                NM_ERR_NOCONV = -4, NM_ERR_TIMEOUT = -5, NM_ERR_NUMERIC = -6
   integer(c_int), parameter :: NM_PREC_FP64 = 0, NM_PREC_MIXED = 1
+  ! phases of the progress callback, subroutine progress(data, phase, done, total) bind(C)
+  integer(c_int), parameter :: NM_PHASE_BOUNDS = 0, NM_PHASE_LANCZOS = 1, NM_PHASE_RITZ = 2, &
+                               NM_PHASE_REFINE = 3, NM_PHASE_DONE = 4
 
   type, bind(C) :: nm_csr
     integer(c_int) :: nrows, ncols
@@ -33,6 +36,10 @@ module nmgpu_mod
     integer(c_int) :: mlan_bounds
     real(c_double) :: ab_bounds(2)
     integer(c_int) :: damping, want_vectors, unscale, use_graph, block, polish
+    real(c_double) :: resid_tol
+    integer(c_int) :: refine_sweeps, refine_maxdeg
+    type(c_funptr) :: progress
+    type(c_ptr) :: progress_data
   end type nm_solve_opts
 
   type, bind(C) :: nm_result
@@ -45,6 +52,9 @@ module nmgpu_mod
     real(c_double) :: t_bounds, t_filter_design, t_lanczos, t_ritz, t_total
     integer(c_long_long) :: n_amv, n_bsolve, n_spmv, n_kernels
     real(c_double) :: t_filter, t_orth, t_eig
+    integer(c_int) :: refine_passes, refine_blocks, refine_maxdeg
+    integer(c_long_long) :: refine_steps
+    real(c_double) :: res2_before_refine
   end type nm_result
 
   type, bind(C) :: nm_slice

@@ -53,7 +53,10 @@ def main(argv=None) -> None:
                      "err_ref_max": float(r.err_ref.max()) if len(r.lam) else None,
                      "err_ref_median": float(np.median(r.err_ref)) if len(r.lam) else None,
                      "res2_max": float(r.res2.max()) if len(r.lam) else None,
-                     "res2_median": float(np.median(r.res2)) if len(r.lam) else None}
+                     "res2_median": float(np.median(r.res2)) if len(r.lam) else None,
+                     "gated_1e-10": int((r.err_ref <= 1e-10).sum()),
+                     "refinement": {k: r.counts[k] for k in ("refine_passes", "refine_blocks", "refine_maxdeg",
+                                                             "refine_steps", "res2_before_refine")}}
     m = res["mixed"].lam
     f = np.load(a.fp64_lam) if a.fp64_lam else res["fp64"].lam
     if a.save_fp64_lam and "fp64" in res:

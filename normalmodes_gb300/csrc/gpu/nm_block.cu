@@ -839,13 +839,13 @@ __global__ void k_to_colmajor(const XT* __restrict__ blk, int n, double* __restr
 }
 
 template <typename XT>
-__global__ void k_from_colmajor(const double* __restrict__ src, size_t ld, int n, XT* __restrict__ blk) {
+__global__ void k_from_colmajor(const double* __restrict__ src, size_t ld, int n, int ncol, XT* __restrict__ blk) {
   __shared__ double tile[kBlk][kBlk + 1];
   const int i0 = blockIdx.x * kBlk;
   const int tx = threadIdx.x, ty = threadIdx.y;
   for (int c = ty; c < kBlk; c += 8) {
     const int i = i0 + tx;
-    tile[c][tx] = i < n ? src[(size_t)c * ld + i] : 0.0;
+    tile[c][tx] = i < n && c < ncol ? src[(size_t)c * ld + i] : 0.0;  // columns >= ncol read as zero
   }
   __syncthreads();
   for (int r = ty; r < kBlk; r += 8) {
@@ -1150,7 +1150,7 @@ __global__ void k_force(float* __restrict__ v, const float* __restrict__ R, cons
   v[i] = fmaf(f[i & (kBlk - 1)], R[i], v[i]);
 }
 // U(:, col) += sc_col G(:, col): G row-major 32-column block, U column-major
-__global__ void k_add_colmajor(const float* __restrict__ G, const double* __restrict__ sc, int n,
+__global__ void k_add_colmajor(const float* __restrict__ G, const double* __restrict__ sc, int n, int ncol,
                                double* __restrict__ U, size_t ld) {
   __shared__ float tile[kBlk][kBlk + 1];
   const int i0 = blockIdx.x * kBlk;
@@ -1160,12 +1160,63 @@ __global__ void k_add_colmajor(const float* __restrict__ G, const double* __rest
     tile[r][tx] = i < n ? G[(size_t)i * kBlk + tx] : 0.0f;
   }
   __syncthreads();
-  for (int c = ty; c < kBlk; c += 8) {
+  for (int c = ty; c < ncol; c += 8) {
     const int i = i0 + tx;
     if (i < n) U[(size_t)c * ld + i] += sc[c] * (double)tile[tx][c];
   }
 }
 }  // namespace
+
+namespace {
+// Per-column sums of a row-major 32-column FP64 block pair, in a fixed order:
+// stage 1, CTA b sums rows b, b + G, b + 2G, ... (one warp per row, lane =
+// column) into part[b][0:32] = sum (AU - theta BU)^2, part[b][32:64] =
+// sum U BU; stage 2 adds the G partial sums in CTA order.
+constexpr int kColRedCtas = 512;
+__global__ void __launch_bounds__(256) k_colres_part(const double* __restrict__ AU, const double* __restrict__ BU,
+                                                     const double* __restrict__ U, const double* __restrict__ theta,
+                                                     int rows, double* __restrict__ part) {
+  __shared__ double sr[8][kBlk], su[8][kBlk];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const double th = theta[lane];
+  double r2 = 0.0, ub = 0.0;
+  for (int i = blockIdx.x * 8 + w; i < rows; i += gridDim.x * 8) {
+    const size_t o = (size_t)i * kBlk + lane;
+    const double bu = BU[o];
+    const double r = fma(-th, bu, AU[o]);
+    r2 = fma(r, r, r2);
+    ub = fma(U[o], bu, ub);
+  }
+  sr[w][lane] = r2;
+  su[w][lane] = ub;
+  __syncthreads();
+  if (w == 0) {
+    double a = 0.0, b = 0.0;
+    for (int q = 0; q < 8; ++q) {
+      a += sr[q][lane];
+      b += su[q][lane];
+    }
+    part[(size_t)blockIdx.x * 2 * kBlk + lane] = a;
+    part[(size_t)blockIdx.x * 2 * kBlk + kBlk + lane] = b;
+  }
+}
+__global__ void k_colres_sum(const double* __restrict__ part, int nparts, double* __restrict__ out) {
+  const int t = threadIdx.x;  // 64 threads: 32 residual sums, 32 B-norms
+  double a = 0.0;
+  for (int b = 0; b < nparts; ++b) a += part[(size_t)b * 2 * kBlk + t];
+  out[t] = a;
+}
+}  // namespace
+
+size_t blk_colres_scratch() { return (size_t)kColRedCtas * 2 * kBlk + 2 * kBlk; }
+
+void blk_colres(const double* AU, const double* BU, const double* U, const double* theta, int rows, double* scratch,
+                cudaStream_t s) {
+  const int g = std::max(1, std::min(kColRedCtas, (rows + 7) / 8));
+  k_colres_part<<<g, 256, 0, s>>>(AU, BU, U, theta, rows, scratch);
+  k_colres_sum<<<1, 2 * kBlk, 0, s>>>(scratch, g, scratch + (size_t)kColRedCtas * 2 * kBlk);
+  nmg::add_launches(2);
+}
 
 void blk_resid_f32(const double* AU, const double* BU, const double* theta, float* R, float scale, size_t len,
                    cudaStream_t s) {
@@ -1177,7 +1228,10 @@ void blk_force(float* v, const float* R, const float* f, size_t len, cudaStream_
   nmg::add_launches(1);
 }
 void blk_add_colmajor(const float* G, const double* sc, int n, double* U, size_t ld, cudaStream_t s) {
-  k_add_colmajor<<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(G, sc, n, U, ld);
+  blk_add_colmajor_cols(G, sc, n, kBlk, U, ld, s);
+}
+void blk_add_colmajor_cols(const float* G, const double* sc, int n, int ncol, double* U, size_t ld, cudaStream_t s) {
+  k_add_colmajor<<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(G, sc, n, std::min(ncol, kBlk), U, ld);
   nmg::add_launches(1);
 }
 
@@ -1204,11 +1258,15 @@ void blk_to_colmajor(const XT* blk, int n, double* out, size_t ld, cudaStream_t 
 }
 template <typename XT>
 void blk_from_colmajor(const double* src, size_t ld, int n, XT* blk, cudaStream_t s) {
-  k_from_colmajor<XT><<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(src, ld, n, blk);
+  k_from_colmajor<XT><<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(src, ld, n, kBlk, blk);
   nmg::add_launches(1);
 }
 template void blk_from_colmajor<float>(const double*, size_t, int, float*, cudaStream_t);
 template void blk_from_colmajor<double>(const double*, size_t, int, double*, cudaStream_t);
+void blk_from_colmajor_cols(const double* src, size_t ld, int n, int ncol, double* blk, cudaStream_t s) {
+  k_from_colmajor<double><<<(n + kBlk - 1) / kBlk, dim3(kBlk, 8), 0, s>>>(src, ld, n, std::min(ncol, kBlk), blk);
+  nmg::add_launches(1);
+}
 
 template <typename XT>
 void blk_init_range(XT* vk, XT* vkm1, XT* y, const XT* z, double a1, double mu1, size_t len, cudaStream_t s) {

@@ -155,7 +155,18 @@ void blk_f2d(const float* src, size_t lds, double* dst, size_t ldd, int n, int c
 void blk_resid_f32(const double* AU, const double* BU, const double* theta, float* R, float scale, size_t len,
                    cudaStream_t s);
 void blk_force(float* v, const float* R, const float* f, size_t len, cudaStream_t s);
+// Column sums of row-major 32-column FP64 blocks with `rows` rows: the 64
+// doubles at scratch + blk_colres_scratch() - 64 receive sum_i (AU - theta_c
+// BU)^2 (columns 0..31), then sum_i U BU (32..63); the summation order is
+// fixed, so the result is the same on every run.
+size_t blk_colres_scratch();
+void blk_colres(const double* AU, const double* BU, const double* U, const double* theta, int rows, double* scratch,
+                cudaStream_t s);
 void blk_add_colmajor(const float* G, const double* sc, int n, double* U, size_t ld, cudaStream_t s);
+// The same on the first ncol columns only (the others of U are not touched).
+void blk_add_colmajor_cols(const float* G, const double* sc, int n, int ncol, double* U, size_t ld, cudaStream_t s);
+// blk = src(:, 0:ncol)^T with columns ncol..31 of the row-major block zero.
+void blk_from_colmajor_cols(const double* src, size_t ld, int n, int ncol, double* blk, cudaStream_t s);
 
 // Grouped operators and buffers of the batched path.
 struct BlockState {
@@ -231,5 +242,31 @@ double filter_at_zero(const Pol& pol);
 // three-term recurrence driven by the FP64 residual A U - theta B U and runs
 // in FP32 (it is small, so FP32 rounding stays at FP64 level relative to U).
 int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, const PolishPlan& plan);
+
+// Adaptive refinement of the mixed path (polish = 0), the same correction
+// U <- U + B~^-1 D / T_d(l(theta)) as polish64 driven by the FP64 residual
+// R = A U - theta B U, with the band and degree chosen per block of 32 Ritz
+// vectors from R itself: the band [c, lmax] starts at c = band * (largest
+// theta of the block), and the degree is the smallest that damps every
+// column's residual below tol_res2 with a margin `safety`:
+//   d = max_j acosh(safety res2_j / tol_res2) / acosh(1 + 2 (c - theta_j) / (lmax - c)),
+// clamped to [mindeg, maxdeg]; blocks already below tol_res2 are left alone.
+// Components along modes below c are not damped; the FP64 Rayleigh-Ritz
+// that follows each pass removes those along the other Ritz vectors.
+struct RefineParams {
+  double tol_res2 = 1e-7;  // target ||A u - theta B u||_2 / (|theta| ||u||_B)
+  double band = 2.0;
+  double safety = 4.0;
+  int mindeg = 8, maxdeg = 4000;
+};
+struct RefineStats {
+  int blocks = 0, max_deg = 0;   // blocks refined, largest degree
+  long long steps = 0;           // block degree steps spent
+  double max_res2_before = 0.0;  // largest res2 measured before the pass
+};
+int refine_block_degree(const std::vector<double>& theta, const std::vector<double>& res2, double c0, double lmax,
+                        const RefineParams& rp);
+int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, const RefineParams& rp,
+             RefineStats* stats);
 
 }  // namespace nmg

@@ -896,6 +896,7 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
     if ((rc = gram(Vc, ldw, Wc, ldw, Gh))) return fail(rc);
     add_phase_times();  // gram() synchronised the stream
     nblk = j + 1;
+    progress(c, NM_PHASE_LANCZOS, nblk, max_blocks);
     if (!chol_upper(Gh.data(), S, Rh)) {
       done = true;  // block breakdown: the Krylov space is exhausted
       break;
@@ -1223,6 +1224,151 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
   NM_CUDA(c, cudaMemcpyAsync(U, Up, sizeof(double) * (size_t)n * nc, cudaMemcpyDeviceToDevice, s));
   NM_CUDA(c, cudaGetLastError());
   release();
+  return NM_OK;
+}
+
+int refine_block_degree(const std::vector<double>& theta, const std::vector<double>& res2, double c0, double lmax,
+                        const RefineParams& rp) {
+  double need = 0.0;
+  for (size_t j = 0; j < theta.size() && j < res2.size(); ++j) {
+    const double damp = rp.safety * res2[j] / rp.tol_res2;
+    if (!(damp > 1.0)) continue;
+    const double delta = 2.0 * (c0 - theta[j]) / (lmax - c0);
+    if (!(delta > 0.0)) continue;  // at or above the band: not refinable
+    need = std::max(need, std::acosh(damp) / std::acosh(1.0 + delta));
+  }
+  if (need <= 0.0) return 0;
+  return std::max(rp.mindeg, std::min(rp.maxdeg, (int)std::ceil(need)));
+}
+
+int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, const RefineParams& rp,
+             RefineStats* out) {
+  BlockState* st = bs(c);
+  RefineStats stats;
+  if (!st || !st->ok || nc <= 0 || c->precision != NM_PREC_MIXED) {
+    if (out) *out = stats;
+    return NM_OK;
+  }
+  if ((int)theta.size() < nc || !(lmax > 0.0) || !(rp.tol_res2 > 0.0))
+    return set_err(c, NM_ERR_ARG, "refine: bad arguments");
+  int rc;
+  if ((rc = block_buffers(c))) return rc;
+  const int n = c->n, np = c->np, S = kBlk;
+  const int ncp = (nc + S - 1) / S * S;
+  const int nblk = ncp / S;
+  cudaStream_t s = c->stream;
+  const size_t L = (size_t)S * n, P = (size_t)S * (np ? np : 1);
+  double* p64 = st->f64 + 2 * L;
+  double* sin_ = carve(p64, L);
+  double* sAU = carve(p64, L);
+  double* sBU = carve(p64, 4 * L);
+  double* x0 = carve(p64, P);
+  double* y0 = carve(p64, P);
+  double* apw = carve(p64, 4 * P);
+  FiltBufs<float> f = filt_carve<float>(st->f32, n, np);
+  double *dth = nullptr, *dsc = nullptr, *dred = nullptr;
+  float* dfor = nullptr;
+  auto release = [&]() {
+    cudaStreamSynchronize(s);
+    for (double** q : {&dth, &dsc, &dred}) {
+      cudaFree(*q);
+      *q = nullptr;
+    }
+    cudaFree(dfor);
+    dfor = nullptr;
+  };
+  auto guard = on_exit(release);
+  if (cudaMalloc(&dth, sizeof(double) * S) != cudaSuccess || cudaMalloc(&dsc, sizeof(double) * S) != cudaSuccess ||
+      cudaMalloc(&dred, sizeof(double) * blk_colres_scratch()) != cudaSuccess ||
+      cudaMalloc(&dfor, sizeof(float) * (size_t)S * std::max(rp.maxdeg, 1)) != cudaSuccess) {
+    release();
+    return set_err(c, NM_ERR_OOM, "refinement workspace");
+  }
+  const double* dsums = dred + blk_colres_scratch() - 2 * S;
+  FiltEpi ep0;  // plain product
+  std::vector<double> th(S), sc(S), sums(2 * S);
+  std::vector<float> forc((size_t)S * rp.maxdeg);
+  for (int b = 0; b < nblk; ++b) {
+    const int j0 = b * S, ncol = std::min(S, nc - j0);
+    for (int col = 0; col < S; ++col) th[col] = col < ncol ? theta[j0 + col] : 0.0;
+    NM_CUDA(c, cudaMemcpyAsync(dth, th.data(), sizeof(double) * S, cudaMemcpyHostToDevice, s));
+    // FP64 residual R = A U - theta B U (reference operators and degrees);
+    // the last block's padding columns are zero
+    blk_from_colmajor_cols(U + (size_t)j0 * n, n, n, ncol, sin_, s);
+    if (c->fs) {
+      blk_et<double, double>(st->ET64, sin_, x0, s);
+      blk_ap_solve<double, double>(c, st->Ap64, x0, y0, apw);
+    }
+    blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sAU, nullptr, nullptr, nullptr, ep0, s);
+    blk_mass_spmv<double>(st->M64, sin_, sBU, s);
+    blk_colres(sAU, sBU, sin_, dth, n, dred, s);
+    NM_CUDA(c, cudaMemcpyAsync(sums.data(), dsums, sizeof(double) * 2 * S, cudaMemcpyDeviceToHost, s));
+    NM_CUDA(c, cudaStreamSynchronize(s));
+    std::vector<double> tb, rb;
+    double thmax = 0.0, worst = 0.0;
+    for (int col = 0; col < ncol; ++col) {
+      const double ub = sums[S + col];
+      const double r2 = ub > 0.0 && th[col] != 0.0 ? std::sqrt(sums[col] / ub) / std::fabs(th[col]) : 0.0;
+      tb.push_back(th[col]);
+      rb.push_back(r2);
+      thmax = std::max(thmax, th[col]);
+      worst = std::max(worst, r2);
+    }
+    stats.max_res2_before = std::max(stats.max_res2_before, worst);
+    const double c0 = std::min(rp.band * thmax, 0.5 * lmax);
+    const int deg = thmax > 0.0 ? refine_block_degree(tb, rb, c0, lmax, rp) : 0;
+    if (deg > 0) {
+      const double alpha = 2.0 / (lmax - c0), beta = (lmax + c0) / (lmax - c0);
+      FiltEpi ep;  // D_{j+1} = 2 alpha A B~^-1 D_j - 2 beta D_j - D_{j-1} (+ forcing)
+      ep.mode = 1;
+      ep.s = 2.0 * alpha;
+      ep.cc = beta / alpha;
+      ep.pm = 1.0;
+      ep.mu = 0.0;
+      for (int col = 0; col < S; ++col) {
+        const double l = alpha * th[col] - beta;
+        const bool skip = col >= ncol || !(l < -1.0 - 1e-12);
+        double tm1 = 1.0, tj = l;
+        for (int j = 1; j < deg; ++j) {
+          forc[(size_t)j * S + col] = skip ? 0.0f : (float)(2.0 * alpha * tj);
+          const double tn = 2.0 * l * tj - tm1;
+          tm1 = tj;
+          tj = tn;
+        }
+        sc[col] = skip || !std::isfinite(tj) ? 0.0 : 1.0 / tj;  // 1 / T_deg(l(theta))
+      }
+      NM_CUDA(c, cudaMemcpyAsync(dsc, sc.data(), sizeof(double) * S, cudaMemcpyHostToDevice, s));
+      NM_CUDA(c, cudaMemcpyAsync(dfor, forc.data(), sizeof(float) * (size_t)S * deg, cudaMemcpyHostToDevice, s));
+      blk_resid_f32(sAU, sBU, dth, f.zin, 1.0f, L, s);
+      blk_resid_f32(sAU, sBU, dth, f.vk, (float)alpha, L, s);
+      NM_CUDA(c, cudaMemsetAsync(f.vkm1, 0, sizeof(float) * L, s));
+      float *vk = f.vk, *vkm1 = f.vkm1, *vkp1 = f.vkp1;
+      for (int j = 1; j < deg; ++j) {
+        blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
+        if (c->fs) {
+          blk_et<float, float>(st->ET32, f.w2, f.x0, s);
+          blk_ap_solve<float, float>(c, st->Ap32, f.x0, f.y0, f.apwork);
+        }
+        blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s);
+        blk_force(vkp1, f.zin, dfor + (size_t)j * S, L, s);
+        float* t = vkm1;
+        vkm1 = vk;
+        vk = vkp1;
+        vkp1 = t;
+      }
+      // U += B~^-1 D_deg / T_deg(l(theta))
+      blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
+      blk_add_colmajor_cols(f.w2, dsc, n, ncol, U + (size_t)j0 * n, n, s);
+      c->n_amv += (long long)deg * S;
+      stats.blocks += 1;
+      stats.steps += deg;
+      stats.max_deg = std::max(stats.max_deg, deg);
+    }
+    NM_CUDA(c, cudaGetLastError());
+    progress(c, NM_PHASE_REFINE, b + 1, nblk);
+  }
+  release();
+  if (out) *out = stats;
   return NM_OK;
 }
 

@@ -113,6 +113,9 @@ struct nm_ctx {
   // block (batched) path: grouped operators and buffers, built on first use
   void* blk = nullptr;  // nmg::BlockState*
   const nm_csr* src[5] = {nullptr};  // not owned; only valid inside nm_create
+  // progress callback of the solve in flight (nm_solve_opts.progress)
+  nm_progress_fn progress = nullptr;
+  void* progress_data = nullptr;
 };
 
 namespace nmg {
@@ -121,6 +124,15 @@ namespace nmg {
 // captured node count).  Read by nm_solve for nm_result.n_kernels.
 long long launches();
 void add_launches(long long k);
+
+// Reports a phase boundary to the solve's progress callback, if any, after
+// the context's stream has drained (so host timestamps taken in the callback
+// cover the device work before it).
+inline void progress(nm_ctx* c, int phase, int done, int total) {
+  if (!c->progress) return;
+  cudaStreamSynchronize(c->stream);
+  c->progress(c->progress_data, phase, done, total);
+}
 
 // Runs f when the scope ends (device scratch released on every return path).
 template <typename F>

@@ -375,6 +375,16 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
   const double t0 = now_s();
   const long long amv0 = c->n_amv, bs0 = c->n_bsolve, sp0 = c->n_spmv, k0 = launches();
   int rc;
+  // the callback is the caller's for this call only
+  struct ProgressScope {
+    nm_ctx* c;
+    ~ProgressScope() {
+      c->progress = nullptr;
+      c->progress_data = nullptr;
+    }
+  } pscope{c};
+  c->progress = o.progress;
+  c->progress_data = o.progress_data;
   // ---- bounds of B^-1 A (src/mod_pevsl.f90:84)
   double lmin, lmax;
   if (o.ab_bounds[1] > 0) {
@@ -385,6 +395,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
     if ((rc = lan_bounds_gen(c, o.mlan_bounds > 0 ? o.mlan_bounds : 3000, 1e-5, &lmin, &lmax, &steps))) return rc;
   }
   if (c->verbose) printf(" step 0: eigenvalue bounds for B^{-1}A: lmin %.15g lmax %.15g\n", lmin, lmax);
+  progress(c, NM_PHASE_BOUNDS, 1, 1);
   const double t1 = now_s();
   // ---- interval (src/mod_pevsl.f90:93-103): frequencies are default REAL,
   //      PI the single-precision literal 3.14159265359 widened to real*8.
@@ -417,9 +428,9 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
       return rc;
     // FP32 filter: close Ritz pairs are mixed at the FP32 noise level; an
     // FP64 Rayleigh-Ritz over the Ritz block separates them.
-    if (mixed) {
-      // FP64-accurate refinement of the Ritz vectors between two
-      // Rayleigh-Ritz passes (plan: degree, band, see polish_plan)
+    if (mixed && o.polish > 0) {
+      // fixed refinement plan between two Rayleigh-Ritz passes (degree,
+      // band: polish_plan)
       const PolishPlan plan = polish_plan(res->xintv, o.polish);
       const bool refine = plan.refine && nc > 0;
       std::vector<double> theta;
@@ -429,12 +440,48 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
         cudaFree(U);
         return rc;
       }
+      progress(c, NM_PHASE_RITZ, nc, nc);
       if (refine) {
         if ((rc = polish64(c, U, nc, theta, res->xintv[3], plan)) ||
             (rc = rayleigh_ritz64(c, &U, nc))) {
           cudaFree(U);
           return rc;
         }
+      }
+    } else if (mixed) {
+      // adaptive refinement: passes of refine64 (degree per block from the
+      // measured FP64 residuals), each closed by an FP64 Rayleigh-Ritz,
+      // until every block is below the target (or the pass limit)
+      const bool refine = o.polish == 0 && nc > 0;
+      std::vector<double> theta;
+      if ((rc = rayleigh_ritz64(c, &U, nc, &theta, refine))) {
+        cudaFree(U);
+        return rc;
+      }
+      progress(c, NM_PHASE_RITZ, nc, nc);
+      RefineParams rp;
+      rp.tol_res2 = (o.resid_tol > 0 ? o.resid_tol : 1e-10) * std::sqrt((double)n);  // err_ref = res2 / sqrt(N)
+      if (o.refine_maxdeg > 0) rp.maxdeg = o.refine_maxdeg;
+      const int sweeps = o.refine_sweeps > 0 ? o.refine_sweeps : 2;
+      for (int sw = 0; refine && sw < sweeps; ++sw) {
+        RefineStats rs;
+        if ((rc = refine64(c, U, nc, theta, res->xintv[3], rp, &rs))) {
+          cudaFree(U);
+          return rc;
+        }
+        res->refine_blocks += rs.blocks;
+        res->refine_steps += rs.steps;
+        res->refine_maxdeg = std::max(res->refine_maxdeg, rs.max_deg);
+        if (sw == 0) res->res2_before_refine = rs.max_res2_before;
+        if (c->verbose)
+          printf(" refinement pass %d: %d blocks, %lld block degree steps (max degree %d), res2 before %.3e\n",
+                 sw + 1, rs.blocks, rs.steps, rs.max_deg, rs.max_res2_before);
+        if (rs.blocks == 0) break;
+        if ((rc = rayleigh_ritz64(c, &U, nc, &theta))) {
+          cudaFree(U);
+          return rc;
+        }
+        ++res->refine_passes;
       }
     }
     res->lanczos_steps = steps;
@@ -510,6 +557,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
     dev_scale(V.col(k + 1), vnew, 1.0 / beta, n, c->stream);
     dev_scale(Z.col(k + 1), znew, 1.0 / beta, n, c->stream);
     eT.push_back(beta);
+    progress(c, NM_PHASE_LANCZOS, kdim, maxit);  // dot_sync drained the stream
     if ((k < 50 || (k - 50) % 50 != 0) && k != maxit - 1) continue;
     std::vector<double> e(eT.begin(), eT.begin() + (kdim - 1));
     std::vector<double> ev = tri_eigs_above(dT, e, pol.bar - eps);
@@ -543,6 +591,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
     NM_CUDA(c, cudaStreamSynchronize(c->stream));
     cudaFree(dS);
   }
+  progress(c, NM_PHASE_RITZ, nc, nc);
   }  // single-vector path
   // ---- Rayleigh quotients, interval test and residuals of the Ritz vectors
   std::vector<double> lam, errv, res2v;
@@ -609,6 +658,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
   res->n_bsolve = c->n_bsolve - bs0;
   res->n_spmv = c->n_spmv - sp0;
   res->n_kernels = launches() - k0;
+  progress(c, NM_PHASE_DONE, nev, nev);
   if (c->verbose) {
     printf(" Relative errors: from the smallest to largest eigens:\n");
     for (int j = 0; j < nev; ++j) printf(" Row %d  relative err. %.6e\n", j + 1, res->err_ref[j]);

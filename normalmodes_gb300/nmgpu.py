@@ -49,7 +49,13 @@ class NmSolveOpts(C.Structure):
     _fields_ = [("maxit", C.c_int), ("tol", C.c_double), ("thresh_int", C.c_double), ("thresh_ext", C.c_double),
                 ("mlan_bounds", C.c_int), ("ab_bounds", C.c_double * 2), ("damping", C.c_int),
                 ("want_vectors", C.c_int), ("unscale", C.c_int), ("use_graph", C.c_int), ("block", C.c_int),
-                ("polish", C.c_int)]
+                ("polish", C.c_int), ("resid_tol", C.c_double), ("refine_sweeps", C.c_int),
+                ("refine_maxdeg", C.c_int), ("progress", C.c_void_p), ("progress_data", C.c_void_p)]
+
+
+# void (*)(void* data, int phase, int done, int total)
+NM_PROGRESS_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_int)
+NM_PHASE_BOUNDS, NM_PHASE_LANCZOS, NM_PHASE_RITZ, NM_PHASE_REFINE, NM_PHASE_DONE = range(5)
 
 
 class NmResult(C.Structure):
@@ -61,7 +67,8 @@ class NmResult(C.Structure):
                 ("t_ritz", C.c_double), ("t_total", C.c_double),
                 ("n_amv", C.c_longlong), ("n_bsolve", C.c_longlong), ("n_spmv", C.c_longlong),
                 ("n_kernels", C.c_longlong), ("t_filter", C.c_double), ("t_orth", C.c_double),
-                ("t_eig", C.c_double)]
+                ("t_eig", C.c_double), ("refine_passes", C.c_int), ("refine_blocks", C.c_int),
+                ("refine_maxdeg", C.c_int), ("refine_steps", C.c_longlong), ("res2_before_refine", C.c_double)]
 
 
 class NmElemModel(C.Structure):
@@ -328,9 +335,15 @@ class Solver:
 
     @staticmethod
     def _solve_opts(maxit=0, tol=0.0, ab_bounds=None, want_vectors=True, unscale=False, use_graph=True, damping=1,
-                    mlan_bounds=0, block=0, polish=0) -> "NmSolveOpts":
+                    mlan_bounds=0, block=0, polish=0, resid_tol=0.0, refine_sweeps=0, refine_maxdeg=0,
+                    progress=None) -> "NmSolveOpts":
         o = NmSolveOpts()
         lib().nm_default_solve_opts(C.byref(o))
+        o.resid_tol = resid_tol
+        o.refine_sweeps = refine_sweeps
+        o.refine_maxdeg = refine_maxdeg
+        if progress is not None:  # an NM_PROGRESS_FN the caller keeps alive for the call
+            o.progress = C.cast(progress, C.c_void_p)
         o.maxit = maxit
         o.tol = tol
         o.want_vectors = int(want_vectors)
@@ -356,14 +369,25 @@ class Solver:
                            {"bounds": r.t_bounds, "filter_design": r.t_filter_design, "lanczos": r.t_lanczos,
                             "ritz": r.t_ritz, "total": r.t_total, "filter": r.t_filter, "orth": r.t_orth,
                             "eig": r.t_eig},
-                           {"amv": r.n_amv, "bsolve": r.n_bsolve, "spmv": r.n_spmv, "kernels": r.n_kernels})
+                           {"amv": r.n_amv, "bsolve": r.n_bsolve, "spmv": r.n_spmv, "kernels": r.n_kernels,
+                            "refine_passes": r.refine_passes, "refine_blocks": r.refine_blocks,
+                            "refine_maxdeg": r.refine_maxdeg, "refine_steps": r.refine_steps,
+                            "res2_before_refine": r.res2_before_refine})
 
     def solve(self, lowfreq: float, upfreq: float, maxit: int = 0, tol: float = 0.0, ab_bounds=None,
               want_vectors: bool = True, unscale: bool = False, use_graph: bool = True, damping: int = 1,
-              mlan_bounds: int = 0, allow_noconv: bool = False, block: int = 0, polish: int = 0) -> SolveResult:
+              mlan_bounds: int = 0, allow_noconv: bool = False, block: int = 0, polish: int = 0,
+              resid_tol: float = 0.0, refine_sweeps: int = 0, refine_maxdeg: int = 0,
+              progress=None) -> SolveResult:
+        """nm_solve on [lowfreq, upfreq] mHz.  `progress`, if given, is a
+        Python callable progress(phase, done, total) called at the solve's
+        phase and block boundaries (NM_PHASE_*), stream drained."""
         L = lib()
+        cb = None
+        if progress is not None:
+            cb = NM_PROGRESS_FN(lambda _d, ph, done, tot: progress(ph, done, tot))
         o = self._solve_opts(maxit, tol, ab_bounds, want_vectors, unscale, use_graph, damping, mlan_bounds, block,
-                             polish)
+                             polish, resid_tol, refine_sweeps, refine_maxdeg, cb)
         r = NmResult()
         rc = L.nm_solve(self._h, lowfreq, upfreq, C.byref(o), C.byref(r))
         try:

@@ -60,7 +60,7 @@ def test_ctypes_mirrors_match_c(c_layout, cname):
 
 
 _FKIND = {"integer(c_int)": (4, 4), "real(c_double)": (8, 8), "integer(c_long_long)": (8, 8),
-          "type(c_ptr)": (8, 8), "integer(c_size_t)": (8, 8)}
+          "type(c_ptr)": (8, 8), "type(c_funptr)": (8, 8), "integer(c_size_t)": (8, 8)}
 
 
 def _fortran_types():

@@ -64,3 +64,16 @@ def test_roofline_inputs(bench):
     d = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
     assert tr == float(d["k_mass_cheb_block32_fp32"]["bytes_per_launch"]) > 0
     assert bench.traffic_per_launch("no_such_kernel") is None
+
+
+def test_step_cuts(bench):
+    """The K steps of the timed solve: equal shares of the block-Lanczos
+    steps, the set-up in the first step and the closing phases in the last,
+    covering [t0, t_end] exactly."""
+    blocks = [1.0 + 0.5 * i for i in range(1, 41)]  # 40 block steps ending at 1.5 .. 21.0
+    cuts = bench.step_cuts(0.0, 30.0, blocks, 4)
+    assert cuts == [0.0, blocks[9], blocks[19], blocks[29], 30.0]
+    assert len(bench.step_cuts(0.0, 30.0, blocks, 20)) == 21
+    assert bench.step_cuts(0.0, 8.0, blocks[:2], 4) == [0.0, 2.0, 4.0, 6.0, 8.0]
+    c = bench.step_cuts(0.0, 30.0, blocks, 1)
+    assert c == [0.0, 30.0]
