@@ -402,8 +402,9 @@ def main():
     spmv["filter_degree_step_ms"] = round(ms_f, 3)
     spmv["filter_degree_step_GBs"] = round(by_f / ms_f / 1e6, 1)
     winfo = warm.info()
-    tuned = {"mass": {"vector_gathers": winfo.mass_vec, "threads": winfo.mass_threads},
-             "ap": {"vector_gathers": winfo.ap_vec, "threads": winfo.ap_threads}}
+    tuned = {"mass": {"vector_gathers": winfo.mass_vec, "threads": winfo.mass_threads, "sweep": winfo.mass_sweep},
+             "ap": {"vector_gathers": winfo.ap_vec, "threads": winfo.ap_threads, "sweep": winfo.ap_sweep},
+             "a_op": {"threads": winfo.aop_threads, "sweep": winfo.aop_sweep}}
 
     cpu = None
     if rank == 0 and not a.no_cpu:

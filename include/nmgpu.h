@@ -164,7 +164,9 @@ int nm_bsolve_dev(nm_ctx* ctx, const double* x, double* y);
  *  - Rejects n > NM_NOALLOC_MAX_ROWS with NM_ERR_ARG (see nm_last_error).
  *  - The first call on a device looks the scratch address up
  *    (cudaGetSymbolAddress with the context's device current); make that
- *    first call before any stream capture.
+ *    first call before any stream capture.  The address is kept for the
+ *    life of the process: after cudaDeviceReset of that device it is stale,
+ *    so do not call this entry point on a device that was reset.
  *  - Nothing in the scratch has to start at zero: each call writes every
  *    row of its work vectors before reading it.
  *  - All calls on a device share the scratch, across contexts: calls that
@@ -297,6 +299,9 @@ typedef struct {
   /* launch shape of the block filter's mass and Ap Chebyshev gathers picked
    * by the autotuner (vec 1: 16-byte gathers; -1 before the first block use) */
   int mass_vec, mass_threads, ap_vec, ap_threads;
+  /* row schedule of those (1: one contiguous row range per CTA, 0: a few
+   * rows per CTA) and the CTA size / schedule of the block A-op kernels */
+  int mass_sweep, ap_sweep, aop_threads, aop_sweep;
 } nm_info;
 int nm_get_info(nm_ctx* ctx, nm_info* info);
 void* nm_get_stream(nm_ctx* ctx); /* cudaStream_t of the context */

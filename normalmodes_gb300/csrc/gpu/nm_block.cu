@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <cmath>
 #include <cstdlib>
 #include <type_traits>
@@ -262,6 +264,33 @@ namespace {
 constexpr int kT = 256;             // threads per block = 8 rows of 32 lanes
 constexpr int kRowsPerBlock = kT / kBlk;
 inline int nrb(long long rows) { return (int)((rows + kRowsPerBlock - 1) / kRowsPerBlock); }
+constexpr int kTMax = 1024;  // largest CTA of the row kernels (sweep launches)
+
+// Rows a warp computes.  Plain (sweep == 0): CTA b takes rows b*W .. b*W+W-1
+// with W warps, one row per warp.  Sweep: CTA b takes the contiguous range
+// [b*chunk, (b+1)*chunk) and its W warps walk it together (warp w: rows
+// start+w, start+w+W, ...), so the rows in flight on one SM are neighbours
+// along the space-filling curve and their gathered neighbour rows are shared
+// in that SM's L1.  The loop bound is warp-uniform, so shuffles stay legal.
+struct RowRange {
+  int r, end, step;
+};
+__device__ __forceinline__ RowRange row_range(int nrows, int sweep) {
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  RowRange rr;
+  if (sweep) {
+    const int chunk = (nrows + gridDim.x - 1) / gridDim.x;
+    const long long start = (long long)blockIdx.x * chunk;
+    rr.r = (int)min((long long)nrows, start + w);
+    rr.end = (int)min((long long)nrows, start + chunk);
+    rr.step = nw;
+  } else {
+    rr.r = blockIdx.x * nw + w;
+    rr.end = min(nrows, rr.r + 1);
+    rr.step = 1;
+  }
+  return rr;
+}
 
 template <typename XT>
 __device__ __forceinline__ XT fm(XT a, XT b, XT c) {
@@ -291,15 +320,15 @@ __device__ __forceinline__ XT ld(const XT* p) {
 // between them and can be in flight together.  CTAs take consecutive rows;
 // rows are numbered along a space-filling curve, so the rows in flight at
 // any time form a compact piece of the mesh whose neighbour rows stay in L2.
-template <typename VT, typename XT, int NC, int MODE>
-__global__ void __launch_bounds__(kT)
+template <typename VT, typename XT, int NC, int MODE, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1)
     k_mass_cheb(int ng, const int* __restrict__ rp, const int* __restrict__ ci, const VT* __restrict__ mv,
                 const XT* __restrict__ b, const XT* __restrict__ xcur, const XT* xprev, XT* xout, XT a, XT c,
-                XT inv_theta) {
+                XT inv_theta, int sweep) {
   constexpr int UNR = 4;  // gathers in flight per warp
   const int lane = threadIdx.x & (kBlk - 1);
-  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (g >= ng) return;
+  const RowRange rr = row_range(ng, sweep);
+  for (int g = rr.r; g < rr.end; g += rr.step) {
   const XT* src = MODE == 0 ? b : xcur;
   XT bo[NC], xc[NC], xp[NC];
   const size_t i0 = (size_t)NC * g * kBlk + lane;
@@ -350,6 +379,7 @@ __global__ void __launch_bounds__(kT)
     // x_{j+1} = x_j + a (x_j - x_{j-1}) + c (b - M x_j)
     xout[i0 + p * kBlk] = fm<XT>(c, bo[p] - tt, fm<XT>(a, xc[p] - xp[p], xc[p]));
   }
+  }  // rows
 }
 
 // Vector-load variant of the gather Chebyshev step (same recurrence, MODE
@@ -391,11 +421,11 @@ __device__ __forceinline__ VT4 ldv(const VT4* p) {
   return __ldg(p);
 }
 
-template <typename VT, typename XT, int NC, int MODE>
-__global__ void __launch_bounds__(kT)
+template <typename VT, typename XT, int NC, int MODE, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1)
     k_gcheb(int ng, const int* __restrict__ rp, const int* __restrict__ ci, const VT* __restrict__ mv,
             const XT* __restrict__ b, const XT* __restrict__ xcur, const XT* xprev, XT* xout, XT a, XT c,
-            XT inv_theta) {
+            XT inv_theta, int sweep) {
   using V4 = typename Vec16<XT>::T;
   constexpr int V = Vec16<XT>::V;
   constexpr int LPN = kBlk / V;      // lanes per neighbour row (per component)
@@ -403,8 +433,8 @@ __global__ void __launch_bounds__(kT)
   constexpr int RW = NC * kBlk;      // values per block row
   const int lane = threadIdx.x & 31;
   const int q = lane / LPN, i = lane % LPN;
-  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (g >= ng) return;
+  const RowRange rr = row_range(ng, sweep);
+  for (int g = rr.r; g < rr.end; g += rr.step) {
   const XT* src = MODE == 0 ? b : xcur;
   XT acc[NC][V];
 #pragma unroll
@@ -475,6 +505,7 @@ __global__ void __launch_bounds__(kT)
     }
     *reinterpret_cast<V4*>(xout + o) = out;
   }
+  }  // rows
 }
 
 // Staged (tiled) three-term Chebyshev step on a block with NC components
@@ -585,12 +616,13 @@ __global__ void __launch_bounds__(kT) k_mass_spmv(int ng, const int* __restrict_
 }
 
 // x0(k, lane) = sum_entries sum_q et_q w(3h+q, lane)   (pressure rows)
-template <typename VT, typename XT>
-__global__ void __launch_bounds__(kT) k_et(int np, const int* __restrict__ rp, const int* __restrict__ ci,
-                                           const VT* __restrict__ v3, const XT* __restrict__ w, XT* __restrict__ x0) {
+template <typename VT, typename XT, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) k_et(int np, const int* __restrict__ rp, const int* __restrict__ ci,
+                                              const VT* __restrict__ v3, const XT* __restrict__ w,
+                                              XT* __restrict__ x0, int sweep) {
   const int lane = threadIdx.x & (kBlk - 1);
-  const int k = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5);
-  if (k >= np) return;
+  const RowRange rr = row_range(np, sweep);
+  for (int k = rr.r; k < rr.end; k += rr.step) {
   XT s = 0;
   const int e0 = rp[k], e1 = rp[k + 1];
   for (int base = e0; base < e1; base += kBlk) {
@@ -623,6 +655,7 @@ __global__ void __launch_bounds__(kT) k_et(int np, const int* __restrict__ rp, c
     }
   }
   x0[(size_t)k * kBlk + lane] = s;
+  }  // rows
 }
 
 __device__ __forceinline__ bool gbar(GridBar* bar, unsigned nblocks, int* status) {
@@ -724,16 +757,16 @@ __global__ void __launch_bounds__(kTP)
 }
 
 // w(3g+p) = sum_h A_gh(p, :) v(3h + :) [+ sum_k E_gk(p) y(k)]; epilogue as k_amv.
-template <typename VT, typename XT, bool HAS_E, int MODE>
-__global__ void __launch_bounds__(kT)
+template <typename VT, typename XT, bool HAS_E, int MODE, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1)
     k_amv3(int ng, const int* __restrict__ arp, const int* __restrict__ aci, const VT* __restrict__ av,
            const int* __restrict__ erp, const int* __restrict__ eci, const VT* __restrict__ ev,
            const XT* __restrict__ v, const XT* __restrict__ y, XT* __restrict__ out, const XT* __restrict__ vk,
            const XT* __restrict__ vkm1, XT* __restrict__ yacc, XT s, XT cc, XT pm, XT mu,
-           const XT* __restrict__ fz, XT fco) {
+           const XT* __restrict__ fz, XT fco, int sweep) {
   const int lane = threadIdx.x & (kBlk - 1);
-  const int g = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5);
-  if (g >= ng) return;
+  const RowRange rr = row_range(ng, sweep);
+  for (int g = rr.r; g < rr.end; g += rr.step) {
   XT w0 = 0, w1 = 0, w2 = 0;
   const int a0 = arp[g], a1 = arp[g + 1];
   for (int base = a0; base < a1; base += kBlk) {
@@ -801,6 +834,7 @@ __global__ void __launch_bounds__(kT)
       yacc[idx] = fm<XT>(mu, t, yacc[idx]);
     }
   }
+  }  // rows
 }
 
 // blk(i, c) = Z(:, j0 + c)(i) through a 32 x 32 shared-memory tile.
@@ -906,6 +940,42 @@ bool gather_vec(int nc) {
   return v < 0 ? nc == 1 : v != 0;
 }
 
+// Grid of a launch with `thr` threads per CTA over `nrows` rows: one row per
+// warp (plain), or for a sweep the CTAs of `fn` that fit on the GPU at once
+// (occupancy API, cached per kernel and CTA size), each taking one
+// contiguous range of rows.
+int row_grid(const void* fn, int thr, int nrows, int sweep) {
+  const int rows = thr / 32;
+  const int plain = (nrows + rows - 1) / rows;
+  if (!sweep) return std::max(1, plain);
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> cache;
+  int per_gpu = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find({fn, thr});
+    if (it != cache.end()) {
+      per_gpu = it->second;
+    } else {
+      int dev = 0, sms = 0, per = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, thr, 0) != cudaSuccess || per < 1) {
+        cudaGetLastError();
+        per = 1;
+      }
+      per_gpu = std::max(1, sms) * per;
+      cache[{fn, thr}] = per_gpu;
+    }
+  }
+  return std::max(1, std::min(per_gpu, plain));
+}
+
+int launch_threads(const GatherCfg& cfg) {
+  const int cap = cfg.sweep ? kTMax : kT;
+  return std::min(cap, std::max(32, cfg.threads / 32 * 32));
+}
+
 template <typename VT, typename XT, int NC>
 void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s,
                  const GatherCfg& cfg) {
@@ -915,19 +985,33 @@ void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT*
   XT* buf[2] = {work, work + len};  // x_j lives in buf[j & 1]
   const XT it = (XT)ch.inv_theta;
   const bool vec = cfg.vec < 0 ? gather_vec(NC) : cfg.vec != 0;
-  const int thr = std::getenv("NM_GATHER_THREADS") ? gather_threads()
-                                                    : std::min(kT, std::max(32, cfg.threads / 32 * 32));
-  const int rows = thr / 32;
-  const int grid = (ng + rows - 1) / rows;
+  const int thr = std::getenv("NM_GATHER_THREADS") ? gather_threads() : launch_threads(cfg);
+  const int sw = std::getenv("NM_GATHER_THREADS") ? 0 : cfg.sweep;
+  const bool big = thr > kT;  // CTAs above 256 threads use the kernels compiled for 1024
+  const void* fn = vec ? (big ? (const void*)k_gcheb<VT, XT, NC, 2, kTMax> : (const void*)k_gcheb<VT, XT, NC, 2, kT>)
+                       : (big ? (const void*)k_mass_cheb<VT, XT, NC, 2, kTMax>
+                              : (const void*)k_mass_cheb<VT, XT, NC, 2, kT>);
+  const int grid = row_grid(fn, thr, ng, sw);
   for (int j = 1; j <= ch.deg; ++j) {
     const XT a = (XT)ch.a[j - 1], c = (XT)ch.c[j - 1];
     XT* out = j == ch.deg ? x : buf[(j + 1) & 1];
     const XT* cur = buf[j & 1];
     const XT* prev = buf[(j + 1) & 1];
-#define NM_MV(MODE) \
-  k_gcheb<VT, XT, NC, MODE><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it)
-#define NM_MC(MODE) \
-  k_mass_cheb<VT, XT, NC, MODE><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it)
+#define NM_MV(MODE)                                                                                            \
+  do {                                                                                                         \
+    if (big)                                                                                                   \
+      k_gcheb<VT, XT, NC, MODE, kTMax><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it, sw); \
+    else                                                                                                       \
+      k_gcheb<VT, XT, NC, MODE, kT><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it, sw);    \
+  } while (0)
+#define NM_MC(MODE)                                                                                           \
+  do {                                                                                                        \
+    if (big)                                                                                                  \
+      k_mass_cheb<VT, XT, NC, MODE, kTMax><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it, \
+                                                                 sw);                                         \
+    else                                                                                                      \
+      k_mass_cheb<VT, XT, NC, MODE, kT><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it, sw); \
+  } while (0)
     if (vec) {
       if (j == 1) NM_MV(0);
       else if (j == 2) NM_MV(1);
@@ -955,14 +1039,28 @@ void blk_ap_cheb(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b, XT* x, XT
   gather_cheb<VT, XT, 1>(Ap, ch, b, x, work, s, cfg);
 }
 
+// Largest L1 (no shared-memory carve-out) for every gather kernel: their
+// neighbour rows are reused from L1, and they use no shared memory but the
+// few bytes of k_colres_part.
+template <typename VT, typename XT, int MAXT>
+void prefer_l1_set() {
+  const void* fs[] = {(const void*)k_mass_cheb<VT, XT, 3, 0, MAXT>, (const void*)k_mass_cheb<VT, XT, 3, 1, MAXT>,
+                      (const void*)k_mass_cheb<VT, XT, 3, 2, MAXT>, (const void*)k_mass_cheb<VT, XT, 1, 0, MAXT>,
+                      (const void*)k_mass_cheb<VT, XT, 1, 1, MAXT>, (const void*)k_mass_cheb<VT, XT, 1, 2, MAXT>,
+                      (const void*)k_gcheb<VT, XT, 3, 0, MAXT>,     (const void*)k_gcheb<VT, XT, 3, 1, MAXT>,
+                      (const void*)k_gcheb<VT, XT, 3, 2, MAXT>,     (const void*)k_gcheb<VT, XT, 1, 0, MAXT>,
+                      (const void*)k_gcheb<VT, XT, 1, 1, MAXT>,     (const void*)k_gcheb<VT, XT, 1, 2, MAXT>,
+                      (const void*)k_amv3<VT, XT, true, 0, MAXT>,   (const void*)k_amv3<VT, XT, true, 1, MAXT>,
+                      (const void*)k_amv3<VT, XT, false, 0, MAXT>,  (const void*)k_amv3<VT, XT, false, 1, MAXT>,
+                      (const void*)k_et<VT, XT, MAXT>};
+  for (const void* f : fs) cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+}
+
 void blk_prefer_l1() {
-  for (const void* f : {(const void*)k_mass_cheb<float, float, 3, 0>, (const void*)k_mass_cheb<float, float, 3, 1>,
-                        (const void*)k_mass_cheb<float, float, 3, 2>, (const void*)k_mass_cheb<float, float, 1, 0>,
-                        (const void*)k_mass_cheb<float, float, 1, 1>, (const void*)k_mass_cheb<float, float, 1, 2>,
-                        (const void*)k_mass_cheb<double, double, 3, 0>, (const void*)k_mass_cheb<double, double, 3, 1>,
-                        (const void*)k_mass_cheb<double, double, 3, 2>, (const void*)k_mass_cheb<double, double, 1, 0>,
-                        (const void*)k_mass_cheb<double, double, 1, 1>, (const void*)k_mass_cheb<double, double, 1, 2>})
-    cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  prefer_l1_set<float, float, kT>();
+  prefer_l1_set<float, float, kTMax>();
+  prefer_l1_set<double, double, kT>();
+  prefer_l1_set<double, double, kTMax>();
   cudaGetLastError();
 }
 
@@ -1016,8 +1114,15 @@ void blk_mass_spmv(const GCsr<VT>& M, const double* x, double* y, cudaStream_t s
 }
 
 template <typename VT, typename XT>
-void blk_et(const GCsr<VT>& ET, const XT* w, XT* x0, cudaStream_t s) {
-  k_et<VT, XT><<<nrb(ET.nrows), kT, 0, s>>>(ET.nrows, ET.rp, ET.ci, ET.v, w, x0);
+void blk_et(const GCsr<VT>& ET, const XT* w, XT* x0, cudaStream_t s, const GatherCfg& cfg) {
+  const int thr = launch_threads(cfg);
+  if (thr > kT) {
+    const int grid = row_grid((const void*)k_et<VT, XT, kTMax>, thr, ET.nrows, cfg.sweep);
+    k_et<VT, XT, kTMax><<<grid, thr, 0, s>>>(ET.nrows, ET.rp, ET.ci, ET.v, w, x0, cfg.sweep);
+  } else {
+    const int grid = row_grid((const void*)k_et<VT, XT, kT>, thr, ET.nrows, cfg.sweep);
+    k_et<VT, XT, kT><<<grid, thr, 0, s>>>(ET.nrows, ET.rp, ET.ci, ET.v, w, x0, cfg.sweep);
+  }
   nmg::add_launches(1);
 }
 
@@ -1085,16 +1190,26 @@ int blk_coop_blocks() {
 
 template <typename VT, typename XT>
 void blk_amv(const GCsr<VT>& A, const GCsr<VT>* E, const XT* v, const XT* y, XT* out, const XT* vk, const XT* vkm1,
-             XT* yacc, const FiltEpi& ep, cudaStream_t s) {
+             XT* yacc, const FiltEpi& ep, cudaStream_t s, const GatherCfg& cfg) {
   const int ng = A.nrows;
+  const int thr = launch_threads(cfg), sw = cfg.sweep;
+  const bool big = thr > kT;
+  const int grid = row_grid(big ? (const void*)k_amv3<VT, XT, true, 1, kTMax> : (const void*)k_amv3<VT, XT, true, 1, kT>,
+                            thr, ng, sw);
   const XT S = (XT)ep.s, CC = (XT)ep.cc, PM = (XT)ep.pm, MU = (XT)ep.mu, FC = (XT)ep.fco;
   const XT* FZ = (const XT*)ep.fz;
   const int* erp = E ? E->rp : nullptr;
   const int* eci = E ? E->ci : nullptr;
   const VT* ev = E ? E->v : nullptr;
 #define NM_AMV(HE, MO)                                                                                            \
-  k_amv3<VT, XT, HE, MO><<<nrb(ng), kT, 0, s>>>(ng, A.rp, A.ci, A.v, erp, eci, ev, v, y, out, vk, vkm1, yacc, S, \
-                                                CC, PM, MU, FZ, FC)
+  do {                                                                                                            \
+    if (big)                                                                                                      \
+      k_amv3<VT, XT, HE, MO, kTMax><<<grid, thr, 0, s>>>(ng, A.rp, A.ci, A.v, erp, eci, ev, v, y, out, vk, vkm1,    \
+                                                         yacc, S, CC, PM, MU, FZ, FC, sw);                         \
+    else                                                                                                          \
+      k_amv3<VT, XT, HE, MO, kT><<<grid, thr, 0, s>>>(ng, A.rp, A.ci, A.v, erp, eci, ev, v, y, out, vk, vkm1, yacc, \
+                                                      S, CC, PM, MU, FZ, FC, sw);                                  \
+  } while (0)
   if (E) {
     if (ep.mode == 0) NM_AMV(true, 0);
     else NM_AMV(true, 1);
@@ -1290,11 +1405,11 @@ void blk_init_filter(XT* vk, XT* vkm1, XT* y, const XT* v, double mu0, size_t le
                                       const GatherCfg&);                                                           \
   template void blk_ap_cheb<VT, XT>(const GCsr<VT>&, const ChebSetup&, const XT*, XT*, XT*, cudaStream_t,            \
                                     const GatherCfg&);                                                             \
-  template void blk_et<VT, XT>(const GCsr<VT>&, const XT*, XT*, cudaStream_t);                                     \
+  template void blk_et<VT, XT>(const GCsr<VT>&, const XT*, XT*, cudaStream_t, const GatherCfg&);                   \
   template void blk_ap_cheb_persistent<VT, XT>(const GCsr<VT>&, const ChebSetup&, const XT*, XT*, XT*, GridBar*,   \
                                                int*, int, cudaStream_t);                                           \
   template void blk_amv<VT, XT>(const GCsr<VT>&, const GCsr<VT>*, const XT*, const XT*, XT*, const XT*, const XT*, \
-                                XT*, const FiltEpi&, cudaStream_t);
+                                XT*, const FiltEpi&, cudaStream_t, const GatherCfg&);
 NM_INST(double, double)
 NM_INST(float, float)
 #undef NM_INST

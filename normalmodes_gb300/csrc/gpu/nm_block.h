@@ -93,6 +93,12 @@ void free_g(GCsr<T>& g);
 struct GatherCfg {
   int vec = -1;
   int threads = 256;
+  // 0: CTA b takes rows b*W .. b*W+W-1 (W = threads / 32, one per warp);
+  // 1: sweep -- CTA b takes one contiguous range of about rows / grid rows
+  //    and its warps walk it together, grid = the CTAs co-resident on the
+  //    GPU, so the neighbour rows of nearby rows (space-filling-curve order)
+  //    stay in that SM's L1
+  int sweep = 0;
 };
 
 // Block kernels (S = kBlk columns, row-major blocks).
@@ -105,13 +111,13 @@ void blk_ap_cheb(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b, XT* x, XT
 // Prefer L1 over shared memory for the gather kernels (once per context).
 void blk_prefer_l1();
 template <typename VT, typename XT>
-void blk_et(const GCsr<VT>& ET, const XT* w, XT* x0, cudaStream_t s);
+void blk_et(const GCsr<VT>& ET, const XT* w, XT* x0, cudaStream_t s, const GatherCfg& cfg = GatherCfg());
 template <typename VT, typename XT>
 void blk_ap_cheb_persistent(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b, XT* x, XT* work, GridBar* bar,
                             int* status, int blocks, cudaStream_t s);
 template <typename VT, typename XT>
 void blk_amv(const GCsr<VT>& A, const GCsr<VT>* E, const XT* v, const XT* y, XT* out, const XT* vk, const XT* vkm1,
-             XT* yacc, const FiltEpi& ep, cudaStream_t s);
+             XT* yacc, const FiltEpi& ep, cudaStream_t s, const GatherCfg& cfg = GatherCfg());
 // Chebyshev solve (three-term form, deg launches) of the block with NC
 // components per row on a tiled matrix: NC = 3 for the mass M (x) I_3,
 // NC = 1 for the pressure matrix Ap.  work holds 2 blocks.
@@ -183,6 +189,7 @@ struct BlockState {
   ChebSetup chB32, chAp32;
   // launch shapes of the gather solves chosen by block_autotune
   GatherCfg gm32, gm64, ga32, ga64;
+  GatherCfg gA32, gA64;  // block A-op (k_et, k_amv3): threads and sweep
   bool tuned = false;
   size_t f32_len = 0, f64_len = 0;
   cublasHandle_t cublas = nullptr;

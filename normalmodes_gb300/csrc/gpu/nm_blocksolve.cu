@@ -185,6 +185,12 @@ const ChebSetup& ap_cheb(nm_ctx* c) {
   return std::is_same<XT, float>::value && st->chAp32.deg > 0 ? st->chAp32 : c->chebAp;
 }
 
+// Launch shape of the block A-op kernels (k_et, k_amv3) picked by the autotuner.
+template <typename XT>
+const GatherCfg& amv_cfg(nm_ctx* c) {
+  return std::is_same<XT, float>::value ? bs(c)->gA32 : bs(c)->gA64;
+}
+
 template <typename VT, typename XT>
 void blk_mass_solve(nm_ctx* c, const GCsr<VT>& M, const XT* b, XT* x, XT* work) {
   BlockState* st = bs(c);
@@ -227,7 +233,7 @@ void block_filter(nm_ctx* c, const Pol& pol, const GCsr<VT>& M, const GCsr<VT>& 
   for (int k = 1; k <= pol.deg; ++k) {
     blk_mass_solve<VT, XT>(c, M, vk, f.w2, f.bwork);
     if (c->fs) {
-      blk_et<VT, XT>(ET, f.w2, f.x0, s);
+      blk_et<VT, XT>(ET, f.w2, f.x0, s, amv_cfg<XT>(c));
       blk_ap_solve<VT, XT>(c, Ap, f.x0, f.y0, f.apwork);
     }
     FiltEpi ep;
@@ -236,7 +242,7 @@ void block_filter(nm_ctx* c, const Pol& pol, const GCsr<VT>& M, const GCsr<VT>& 
     ep.cc = pol.cc;
     ep.pm = k == 1 ? 0.0 : 1.0;
     ep.mu = pol.mu[k];
-    blk_amv<VT, XT>(A, c->fs ? &E : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s);
+    blk_amv<VT, XT>(A, c->fs ? &E : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s, amv_cfg<XT>(c));
     XT* t = vkm1;
     vkm1 = vk;
     vk = vkp1;
@@ -266,7 +272,7 @@ void block_filter_range(nm_ctx* c, const Pol& pol, FiltBufs<float> f, double* si
   for (int k = 1; k < pol.deg; ++k) {
     blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
     if (c->fs) {
-      blk_et<float, float>(st->ET32, f.w2, f.x0, s);
+      blk_et<float, float>(st->ET32, f.w2, f.x0, s, st->gA32);
       blk_ap_solve<float, float>(c, st->Ap32, f.x0, f.y0, f.apwork);
     }
     FiltEpi ep;
@@ -277,7 +283,7 @@ void block_filter_range(nm_ctx* c, const Pol& pol, FiltBufs<float> f, double* si
     ep.mu = pol.mu[k + 1];
     ep.fz = f.zin;
     ep.fco = 2.0 * a1 * tk;
-    blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s);
+    blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s, st->gA32);
     float* t = vkm1;
     vkm1 = vk;
     vk = vkp1;
@@ -290,11 +296,12 @@ void block_filter_range(nm_ctx* c, const Pol& pol, FiltBufs<float> f, double* si
   blk_mass_solve<float, float>(c, st->M32, f.yout, f.w2, f.bwork);
   blk_f2d_flat(f.w2, sin64, L, s);
   if (c->fs) {
-    blk_et<double, double>(st->ET64, sin64, x064, s);
+    blk_et<double, double>(st->ET64, sin64, x064, s, st->gA64);
     blk_ap_solve<double, double>(c, st->Ap64, x064, y064, apw64);
   }
   FiltEpi ep0;
-  blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin64, y064, sout64, nullptr, nullptr, nullptr, ep0, s);
+  blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin64, y064, sout64, nullptr, nullptr,
+                          nullptr, ep0, s, st->gA64);
 }
 
 
@@ -364,11 +371,17 @@ int block_autotune(nm_ctx* c) {
   cudaEvent_t e0, e1;
   NM_CUDA(c, cudaEventCreate(&e0));
   NM_CUDA(c, cudaEventCreate(&e1));
-  const GatherCfg cands[4] = {{0, 256}, {1, 256}, {0, 128}, {1, 128}};
+  // gather shape x CTA size x row schedule (plain: 8 or 4 rows per CTA;
+  // sweep: one contiguous row range per CTA)
+  const GatherCfg cands[8] = {{0, 256, 0},  {1, 256, 0},  {0, 128, 0}, {1, 128, 0},
+                              {0, 1024, 1}, {1, 1024, 1}, {0, 512, 1}, {1, 512, 1}};
+  const GatherCfg acands[3] = {{0, 256, 0}, {0, 1024, 1}, {0, 512, 1}};
   // time one solve (after one untimed run) for every candidate; keep the fastest
-  auto pick = [&](auto&& run, GatherCfg& best) -> int {
+  auto pick = [&](const char* what, auto&& run, GatherCfg& best, bool aop = false) -> int {
     float tbest = 1e30f;
-    for (const GatherCfg& g : cands) {
+    const int ncand = aop ? 3 : 8;
+    for (int ic = 0; ic < ncand; ++ic) {
+      const GatherCfg& g = aop ? acands[ic] : cands[ic];
       run(g);
       NM_CUDA(c, cudaEventRecord(e0, s));
       run(g);
@@ -377,6 +390,9 @@ int block_autotune(nm_ctx* c) {
       NM_CUDA(c, cudaEventSynchronize(e1));
       float ms = 0.f;
       NM_CUDA(c, cudaEventElapsedTime(&ms, e0, e1));
+      if (c->verbose)
+        printf(" autotune candidate %s: vec %d threads %4d sweep %d: %.3f ms\n", what, g.vec, g.threads, g.sweep,
+               0.5 * ms);
       if (ms < tbest) {
         tbest = ms;
         best = g;
@@ -389,34 +405,58 @@ int block_autotune(nm_ctx* c) {
     float* p = st->f32;  // scratch: the FP32 filter buffers (zeroed)
     NM_CUDA(c, cudaMemsetAsync(p, 0, sizeof(float) * (6 * L), s));
     const ChebSetup& chB = st->chB32.deg > 0 ? st->chB32 : c->chebB;
-    if ((rc = pick([&](const GatherCfg& g) { blk_mass_cheb<float, float>(st->M32, chB, p, p + L, p + 2 * L, s, g); },
+    if ((rc = pick("mass fp32",
+                   [&](const GatherCfg& g) { blk_mass_cheb<float, float>(st->M32, chB, p, p + L, p + 2 * L, s, g); },
                    st->gm32)))
       return rc;
     if (c->fs) {
       const ChebSetup& chA = st->chAp32.deg > 0 ? st->chAp32 : c->chebAp;
-      if ((rc = pick([&](const GatherCfg& g) { blk_ap_cheb<float, float>(st->Ap32, chA, p, p + P, p + 2 * P, s, g); },
+      if ((rc = pick("Ap fp32",
+                     [&](const GatherCfg& g) { blk_ap_cheb<float, float>(st->Ap32, chA, p, p + P, p + 2 * P, s, g); },
                      st->ga32)))
         return rc;
     }
+    FiltEpi ep0;  // plain product
+    if ((rc = pick(
+             "A-op fp32",
+             [&](const GatherCfg& g) {
+               if (c->fs) blk_et<float, float>(st->ET32, p, p + 5 * L, s, g);
+               blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, p, p + 5 * L, p + L, nullptr, nullptr,
+                                     nullptr, ep0, s, g);
+             },
+             st->gA32, true)))
+      return rc;
   }
   {
     double* p = st->f64;  // scratch: the FP64 block buffers (zeroed)
     NM_CUDA(c, cudaMemsetAsync(p, 0, sizeof(double) * (6 * L), s));
-    if ((rc = pick([&](const GatherCfg& g) {
+    if ((rc = pick("mass fp64", [&](const GatherCfg& g) {
            blk_mass_cheb<double, double>(st->M64, c->chebB, p, p + L, p + 2 * L, s, g);
          }, st->gm64)))
       return rc;
-    if (c->fs && (rc = pick([&](const GatherCfg& g) {
+    if (c->fs && (rc = pick("Ap fp64", [&](const GatherCfg& g) {
                     blk_ap_cheb<double, double>(st->Ap64, c->chebAp, p, p + P, p + 2 * P, s, g);
                   }, st->ga64)))
+      return rc;
+    FiltEpi ep0;
+    if ((rc = pick(
+             "A-op fp64",
+             [&](const GatherCfg& g) {
+               if (c->fs) blk_et<double, double>(st->ET64, p, p + 5 * L, s, g);
+               blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, p, p + 5 * L, p + L, nullptr, nullptr,
+                                       nullptr, ep0, s, g);
+             },
+             st->gA64, true)))
       return rc;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (c->verbose)
-    printf(" autotune: mass fp32 vec %d x %d, fp64 vec %d x %d; Ap fp32 vec %d x %d, fp64 vec %d x %d\n",
-           st->gm32.vec, st->gm32.threads, st->gm64.vec, st->gm64.threads, st->ga32.vec, st->ga32.threads,
-           st->ga64.vec, st->ga64.threads);
+    printf(" autotune: mass fp32 vec %d x %d sweep %d, fp64 vec %d x %d sweep %d; Ap fp32 vec %d x %d sweep %d, "
+           "fp64 vec %d x %d sweep %d; A-op fp32 %d sweep %d, fp64 %d sweep %d\n",
+           st->gm32.vec, st->gm32.threads, st->gm32.sweep, st->gm64.vec, st->gm64.threads, st->gm64.sweep,
+           st->ga32.vec, st->ga32.threads, st->ga32.sweep, st->ga64.vec, st->ga64.threads, st->ga64.sweep,
+           st->gA32.threads, st->gA32.sweep, st->gA64.threads, st->gA64.sweep);
   return NM_OK;
 }
 
@@ -519,11 +559,11 @@ int block_time_op(nm_ctx* c, int which, int reps, double* ms, double* bytes, int
       if (wantB) blk_mass_solve<float, float>(c, st->M32, f.vk, f.w2, f.bwork);
       if (wantA) {
         if (c->fs) {
-          blk_et<float, float>(st->ET32, f.w2, f.x0, c->stream);
+          blk_et<float, float>(st->ET32, f.w2, f.x0, c->stream, st->gA32);
           blk_ap_solve<float, float>(c, st->Ap32, f.x0, f.y0, f.apwork);
         }
         blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, f.vkp1, f.vk, f.vkm1, f.yout, ep,
-                              c->stream);
+                              c->stream, st->gA32);
       }
     };
   } else {
@@ -533,12 +573,12 @@ int block_time_op(nm_ctx* c, int which, int reps, double* ms, double* bytes, int
       if (wantB) blk_mass_cheb<double, double>(st->M64, c->chebB, f.vk, f.w2, f.bwork, c->stream);
       if (wantA) {
         if (c->fs) {
-          blk_et<double, double>(st->ET64, f.w2, f.x0, c->stream);
+          blk_et<double, double>(st->ET64, f.w2, f.x0, c->stream, st->gA64);
           blk_ap_cheb_persistent<double, double>(st->Ap64, c->chebAp, f.x0, f.y0, f.apwork, c->bar, c->d_status,
                                                  st->coop, c->stream);
         }
         blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, f.w2, f.y0, f.vkp1, f.vk, f.vkm1, f.yout, ep,
-                                c->stream);
+                                c->stream, st->gA64);
       }
     };
   }
@@ -1034,10 +1074,11 @@ int rayleigh_ritz64(nm_ctx* c, double** Uio, int nc, std::vector<double>* theta,
   for (int j0 = 0; j0 < ncp; j0 += S) {
     blk_from_colmajor<double>(Up + (size_t)j0 * n, n, n, sin_, s);
     if (c->fs) {
-      blk_et<double, double>(st->ET64, sin_, x0, s);
+      blk_et<double, double>(st->ET64, sin_, x0, s, st->gA64);
       blk_ap_solve<double, double>(c, st->Ap64, x0, y0, apw);
     }
-    blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sout, nullptr, nullptr, nullptr, ep, s);
+    blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sout, nullptr, nullptr, nullptr,
+                            ep, s, st->gA64);
     blk_to_colmajor<double>(sout, n, AU + (size_t)j0 * n, n, s);
     blk_mass_spmv<double>(st->M64, sin_, sout, s);
     blk_to_colmajor<double>(sout, n, BU + (size_t)j0 * n, n, s);
@@ -1193,10 +1234,11 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
     // FP64 residual R = A U - theta B U (reference operators and degrees)
     blk_from_colmajor<double>(Up + (size_t)j0 * n, n, n, sin_, s);
     if (c->fs) {
-      blk_et<double, double>(st->ET64, sin_, x0, s);
+      blk_et<double, double>(st->ET64, sin_, x0, s, st->gA64);
       blk_ap_solve<double, double>(c, st->Ap64, x0, y0, apw);
     }
-    blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sAU, nullptr, nullptr, nullptr, ep0, s);
+    blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sAU, nullptr, nullptr, nullptr,
+                            ep0, s, st->gA64);
     blk_mass_spmv<double>(st->M64, sin_, sBU, s);
     // FP32: D_0 = 0, D_1 = alpha R;  R kept in zin
     blk_resid_f32(sAU, sBU, dth, f.zin, 1.0f, L, s);
@@ -1206,10 +1248,10 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
     for (int j = 1; j < deg; ++j) {
       blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
       if (c->fs) {
-        blk_et<float, float>(st->ET32, f.w2, f.x0, s);
+        blk_et<float, float>(st->ET32, f.w2, f.x0, s, st->gA32);
         blk_ap_solve<float, float>(c, st->Ap32, f.x0, f.y0, f.apwork);
       }
-      blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s);
+      blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s, st->gA32);
       blk_force(vkp1, f.zin, dfor + (size_t)j * S, L, s);
       float* t = vkm1;
       vkm1 = vk;
@@ -1296,10 +1338,11 @@ int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
     // the last block's padding columns are zero
     blk_from_colmajor_cols(U + (size_t)j0 * n, n, n, ncol, sin_, s);
     if (c->fs) {
-      blk_et<double, double>(st->ET64, sin_, x0, s);
+      blk_et<double, double>(st->ET64, sin_, x0, s, st->gA64);
       blk_ap_solve<double, double>(c, st->Ap64, x0, y0, apw);
     }
-    blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sAU, nullptr, nullptr, nullptr, ep0, s);
+    blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sAU, nullptr, nullptr, nullptr,
+                            ep0, s, st->gA64);
     blk_mass_spmv<double>(st->M64, sin_, sBU, s);
     blk_colres(sAU, sBU, sin_, dth, n, dred, s);
     NM_CUDA(c, cudaMemcpyAsync(sums.data(), dsums, sizeof(double) * 2 * S, cudaMemcpyDeviceToHost, s));
@@ -1346,10 +1389,10 @@ int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
       for (int j = 1; j < deg; ++j) {
         blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
         if (c->fs) {
-          blk_et<float, float>(st->ET32, f.w2, f.x0, s);
+          blk_et<float, float>(st->ET32, f.w2, f.x0, s, st->gA32);
           blk_ap_solve<float, float>(c, st->Ap32, f.x0, f.y0, f.apwork);
         }
-        blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s);
+        blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s, st->gA32);
         blk_force(vkp1, f.zin, dfor + (size_t)j * S, L, s);
         float* t = vkm1;
         vkm1 = vk;

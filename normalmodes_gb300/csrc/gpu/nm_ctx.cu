@@ -295,6 +295,7 @@ int nm_get_info(nm_ctx* c, nm_info* info) {
   info->h2d_bytes = c->h2d_bytes;
   info->device_bytes = c->dev_bytes;
   info->mass_vec = info->mass_threads = info->ap_vec = info->ap_threads = -1;
+  info->mass_sweep = info->ap_sweep = info->aop_threads = info->aop_sweep = -1;
   if (const nmg::BlockState* st = (const nmg::BlockState*)c->blk) {
     if (st->tuned) {
       const bool mixed = c->precision == NM_PREC_MIXED;
@@ -304,6 +305,11 @@ int nm_get_info(nm_ctx* c, nm_info* info) {
       info->mass_threads = gm.threads;
       info->ap_vec = ga.vec;
       info->ap_threads = ga.threads;
+      const nmg::GatherCfg& gA = mixed ? st->gA32 : st->gA64;
+      info->mass_sweep = gm.sweep;
+      info->ap_sweep = ga.sweep;
+      info->aop_threads = gA.threads;
+      info->aop_sweep = gA.sweep;
     }
   }
   return NM_OK;

@@ -20,7 +20,10 @@
 // The device address of g_scratch is looked up once per device with
 // cudaGetSymbolAddress, with the context's device current, on the first call
 // that targets that device; later calls reuse the cached pointer.  That first
-// call on a device should come before any stream capture.
+// call on a device should come before any stream capture.  The address
+// belongs to the device's primary context: cudaDeviceReset (or any other
+// teardown of the primary context) leaves the cached pointer stale, so a
+// process that resets a device must not call this entry point on it again.
 #include <cuda_runtime.h>
 
 #include <mutex>

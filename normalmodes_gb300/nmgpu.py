@@ -149,7 +149,8 @@ class NmInfo(C.Structure):
                 ("nnz_e", C.c_longlong), ("nnz_et", C.c_longlong), ("b_bounds", C.c_double * 2),
                 ("ap_bounds", C.c_double * 2), ("b_cheb_deg", C.c_int), ("ap_cheb_deg", C.c_int),
                 ("t_setup", C.c_double), ("h2d_bytes", C.c_longlong), ("device_bytes", C.c_size_t),
-                ("mass_vec", C.c_int), ("mass_threads", C.c_int), ("ap_vec", C.c_int), ("ap_threads", C.c_int)]
+                ("mass_vec", C.c_int), ("mass_threads", C.c_int), ("ap_vec", C.c_int), ("ap_threads", C.c_int),
+                ("mass_sweep", C.c_int), ("ap_sweep", C.c_int), ("aop_threads", C.c_int), ("aop_sweep", C.c_int)]
 
 
 _lib = None
