@@ -60,6 +60,16 @@ typedef struct {
   double ap_bounds[2]; /* idem for Ap_s                                           */
   int precision;     /* NM_PREC_FP64 or NM_PREC_MIXED (FP32 filter SpMVs)        */
   int verbose;       /* print the reference's progress lines                      */
+  /* Mixed-precision block path; 0 everywhere gives the measured defaults.      */
+  int filter_form;   /* 0: range form W = p(0) Z + A B~^-1 Y (last A-op in FP64,
+                        no FP32 rounding in the zero-frequency modes); 1: the
+                        plain FP32 filter                                        */
+  int orth64;        /* 1: FP64 block Gram-Schmidt (0: FP32 on FP32 basis copies) */
+  double inner_tol;  /* relative accuracy of the FP32 filter's inner B~^-1
+                        Chebyshev solve, which sets its degree (0: 2^-24, FP32;
+                        < 0: the reference's degree)                           */
+  int autotune;      /* 0: time the gather kernels' launch shapes on the first
+                        block use; -1: keep the default shapes                  */
 } nm_opts;
 
 #define NM_PREC_FP64 0

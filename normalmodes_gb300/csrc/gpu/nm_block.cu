@@ -162,92 +162,6 @@ int upload_g(nm_ctx* c, const GCsrHost& h, GCsr<T>& d) {
 template int upload_g<double>(nm_ctx*, const GCsrHost&, GCsr<double>&);
 template int upload_g<float>(nm_ctx*, const GCsrHost&, GCsr<float>&);
 
-bool tile_csr(const GCsrHost& g, int R, TCsrHost& t) {
-  if (g.bs != 1 || R <= 0) return false;
-  t = TCsrHost();
-  t.nrows = g.nrows;
-  t.R = R;
-  t.ntiles = (g.nrows + R - 1) / R;
-  t.rp = g.rp;
-  t.v = g.v;
-  t.li.resize(g.ci.size());
-  std::vector<std::vector<int>> U(t.ntiles);
-  bool ok = true;
-#pragma omp parallel for schedule(dynamic, 64) reduction(&& : ok)
-  for (int k = 0; k < t.ntiles; ++k) {
-    const int r0 = k * R, r1 = std::min(r0 + R, g.nrows);
-    std::vector<int>& u = U[k];
-    u.assign(g.ci.begin() + g.rp[r0], g.ci.begin() + g.rp[r1]);
-    std::sort(u.begin(), u.end());
-    u.erase(std::unique(u.begin(), u.end()), u.end());
-    if (u.size() > 65535) {
-      ok = false;
-      continue;
-    }
-    for (int e = g.rp[r0]; e < g.rp[r1]; ++e)
-      t.li[e] = (uint16_t)(std::lower_bound(u.begin(), u.end(), g.ci[e]) - u.begin());
-  }
-  if (!ok) return false;
-  t.tptr.assign(t.ntiles + 1, 0);
-  for (int k = 0; k < t.ntiles; ++k) {
-    t.tptr[k + 1] = t.tptr[k] + (int)U[k].size();
-    t.maxU = std::max(t.maxU, (int)U[k].size());
-  }
-  t.ulist.resize(t.tptr[t.ntiles]);
-#pragma omp parallel for schedule(static)
-  for (int k = 0; k < t.ntiles; ++k) std::copy(U[k].begin(), U[k].end(), t.ulist.begin() + t.tptr[k]);
-  return true;
-}
-
-int tile_rows_for(const GCsrHost& g, int R0, size_t row_bytes, size_t smem_max, TCsrHost& t) {
-  for (int R = R0; R >= 4; R /= 2) {
-    if (!tile_csr(g, R, t)) continue;
-    if ((size_t)t.maxU * row_bytes <= smem_max) return R;
-  }
-  t = TCsrHost();
-  return 0;
-}
-
-template <typename T>
-int upload_t(nm_ctx* c, const TCsrHost& h, TCsr<T>& d) {
-  free_t(d);
-  d.nrows = h.nrows;
-  d.R = h.R;
-  d.ntiles = h.ntiles;
-  d.maxU = h.maxU;
-  d.nnz = (long long)h.li.size();
-  d.nu = (long long)h.ulist.size();
-  NM_CUDA(c, cudaMalloc(&d.tptr, sizeof(int) * (h.ntiles + 1)));
-  NM_CUDA(c, cudaMalloc(&d.ulist, sizeof(int) * std::max<long long>(d.nu, 1)));
-  NM_CUDA(c, cudaMalloc(&d.rp, sizeof(int) * (h.nrows + 1)));
-  NM_CUDA(c, cudaMalloc(&d.li, sizeof(uint16_t) * std::max<long long>(d.nnz, 1)));
-  NM_CUDA(c, cudaMalloc(&d.v, sizeof(T) * std::max<long long>(d.nnz, 1)));
-  NM_CUDA(c, cudaMemcpy(d.tptr, h.tptr.data(), sizeof(int) * (h.ntiles + 1), cudaMemcpyHostToDevice));
-  if (d.nu) NM_CUDA(c, cudaMemcpy(d.ulist, h.ulist.data(), sizeof(int) * d.nu, cudaMemcpyHostToDevice));
-  NM_CUDA(c, cudaMemcpy(d.rp, h.rp.data(), sizeof(int) * (h.nrows + 1), cudaMemcpyHostToDevice));
-  if (d.nnz) {
-    NM_CUDA(c, cudaMemcpy(d.li, h.li.data(), sizeof(uint16_t) * d.nnz, cudaMemcpyHostToDevice));
-    std::vector<T> tmp(h.v.begin(), h.v.end());
-    NM_CUDA(c, cudaMemcpy(d.v, tmp.data(), sizeof(T) * d.nnz, cudaMemcpyHostToDevice));
-  }
-  c->dev_bytes += d.bytes();
-  return NM_OK;
-}
-template int upload_t<float>(nm_ctx*, const TCsrHost&, TCsr<float>&);
-template int upload_t<double>(nm_ctx*, const TCsrHost&, TCsr<double>&);
-
-template <typename T>
-void free_t(TCsr<T>& t) {
-  cudaFree(t.tptr);
-  cudaFree(t.ulist);
-  cudaFree(t.rp);
-  cudaFree(t.li);
-  cudaFree(t.v);
-  t = TCsr<T>();
-}
-template void free_t<float>(TCsr<float>&);
-template void free_t<double>(TCsr<double>&);
-
 template <typename T>
 void free_g(GCsr<T>& g) {
   cudaFree(g.rp);
@@ -506,92 +420,6 @@ __global__ void __launch_bounds__(MAXT, 1)
     *reinterpret_cast<V4*>(xout + o) = out;
   }
   }  // rows
-}
-
-// Staged (tiled) three-term Chebyshev step on a block with NC components
-// per row; same recurrence and MODE convention as k_mass_cheb.  One CTA per
-// tile of R rows: it first copies the tile's distinct neighbour rows of the
-// gathered block (NC * 32 values each) into shared memory with cp.async
-// (16-byte pieces, all in flight at once), then each warp computes its rows
-// from shared memory (one row per warp, lane = block column; the row's
-// (local column, value) entries are broadcast with shuffles).
-constexpr int kTT = 256;  // threads of the staged kernel
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-}
-
-template <typename VT, typename XT, int NC, int MODE>
-__global__ void __launch_bounds__(kTT)
-    k_tcheb(int nrows, int R, const int* __restrict__ tptr, const int* __restrict__ ulist,
-            const int* __restrict__ rp, const uint16_t* __restrict__ li, const VT* __restrict__ mv,
-            const XT* __restrict__ b, const XT* __restrict__ xcur, const XT* xprev, XT* xout, XT a, XT c,
-            XT inv_theta) {
-  extern __shared__ __align__(16) unsigned char tc_smem[];
-  XT* sx = reinterpret_cast<XT*>(tc_smem);
-  constexpr int RW = NC * kBlk;                 // values per staged row
-  constexpr int V = 16 / (int)sizeof(XT);       // values per 16-byte piece
-  constexpr int PIECES = RW / V;                // pieces per staged row
-  const int tile = blockIdx.x;
-  const int u0 = tptr[tile], nu = tptr[tile + 1] - u0;
-  const XT* src = MODE == 0 ? b : xcur;
-  for (int i = threadIdx.x; i < nu * PIECES; i += kTT) {
-    const int u = i / PIECES, q = i - u * PIECES;
-    const int h = __ldg(ulist + u0 + u);
-    cp_async16(sx + (size_t)u * RW + q * V, src + (size_t)h * RW + q * V);
-  }
-  cp_async_wait_all();
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int r0 = tile * R, r1 = min(r0 + R, nrows);
-  for (int row = r0 + warp; row < r1; row += kTT / 32) {
-    const size_t i0 = (size_t)row * RW + lane;
-    XT bo[NC], xc[NC], xp[NC], t[NC];
-#pragma unroll
-    for (int p = 0; p < NC; ++p) {
-      bo[p] = b[i0 + p * kBlk];
-      xc[p] = MODE == 0 ? bo[p] * inv_theta : xcur[i0 + p * kBlk];
-      xp[p] = MODE == 0 ? (XT)0 : MODE == 1 ? bo[p] * inv_theta : xprev[i0 + p * kBlk];
-      t[p] = 0;
-    }
-    const int e0 = rp[row], e1 = rp[row + 1];
-    for (int base = e0; base < e1; base += 32) {
-      const int cnt = min(32, e1 - base);
-      const int myl = lane < cnt ? (int)__ldg(li + base + lane) : 0;
-      const XT mym = lane < cnt ? (XT)__ldg(mv + base + lane) : (XT)0;
-      int k = 0;
-      for (; k + 4 <= cnt; k += 4) {
-        XT m[4], v[4][NC];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const XT* sp = sx + __shfl_sync(0xffffffffu, myl, k + u) * RW + lane;
-          m[u] = __shfl_sync(0xffffffffu, mym, k + u);
-#pragma unroll
-          for (int p = 0; p < NC; ++p) v[u][p] = sp[p * kBlk];
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int p = 0; p < NC; ++p) t[p] = fm<XT>(m[u], v[u][p], t[p]);
-      }
-      for (; k < cnt; ++k) {
-        const XT* sp = sx + __shfl_sync(0xffffffffu, myl, k) * RW + lane;
-        const XT m = __shfl_sync(0xffffffffu, mym, k);
-#pragma unroll
-        for (int p = 0; p < NC; ++p) t[p] = fm<XT>(m, sp[p * kBlk], t[p]);
-      }
-    }
-#pragma unroll
-    for (int p = 0; p < NC; ++p) {
-      const XT tt = MODE == 0 ? t[p] * inv_theta : t[p];
-      xout[i0 + p * kBlk] = fm<XT>(c, bo[p] - tt, fm<XT>(a, xc[p] - xp[p], xc[p]));
-    }
-  }
 }
 
 template <typename VT>
@@ -917,28 +745,11 @@ __global__ void k_init_filter_blk(XT* vk, XT* vkm1, XT* y, const XT* v, XT mu0, 
 
 }  // namespace
 
-// Threads per CTA of the gather Chebyshev kernel (one row per warp).
-int gather_threads() {
-  static int t = 0;
-  if (!t) {
-    t = kT;
-    if (const char* e = std::getenv("NM_GATHER_THREADS")) t = std::min(kT, std::max(32, std::atoi(e) / 32 * 32));
-  }
-  return t;
-}
-
-// Gather kernel per component count: the 16-byte vector-load kernel
-// (k_gcheb) measured faster for one-component rows (Ap, 128-byte rows), the
-// one-value-per-lane kernel (k_mass_cheb) for the three-component mass rows.
-// NM_GATHER_VEC=0/1 forces one of them for measurements.
-bool gather_vec(int nc) {
-  static int v = -2;
-  if (v == -2) {
-    v = -1;
-    if (const char* e = std::getenv("NM_GATHER_VEC")) v = std::atoi(e) != 0;
-  }
-  return v < 0 ? nc == 1 : v != 0;
-}
+// Default gather kernel per component count when the autotuner has not
+// run: the 16-byte vector-load kernel (k_gcheb) for one-component rows (Ap,
+// 128-byte rows), the one-value-per-lane kernel (k_mass_cheb) for the
+// three-component mass rows.
+bool gather_vec(int nc) { return nc == 1; }
 
 // Grid of a launch with `thr` threads per CTA over `nrows` rows: one row per
 // warp (plain), or for a sweep the CTAs of `fn` that fit on the GPU at once
@@ -985,8 +796,8 @@ void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT*
   XT* buf[2] = {work, work + len};  // x_j lives in buf[j & 1]
   const XT it = (XT)ch.inv_theta;
   const bool vec = cfg.vec < 0 ? gather_vec(NC) : cfg.vec != 0;
-  const int thr = std::getenv("NM_GATHER_THREADS") ? gather_threads() : launch_threads(cfg);
-  const int sw = std::getenv("NM_GATHER_THREADS") ? 0 : cfg.sweep;
+  const int thr = launch_threads(cfg);
+  const int sw = cfg.sweep;
   const bool big = thr > kT;  // CTAs above 256 threads use the kernels compiled for 1024
   const void* fn = vec ? (big ? (const void*)k_gcheb<VT, XT, NC, 2, kTMax> : (const void*)k_gcheb<VT, XT, NC, 2, kT>)
                        : (big ? (const void*)k_mass_cheb<VT, XT, NC, 2, kTMax>
@@ -1064,49 +875,6 @@ void blk_prefer_l1() {
   cudaGetLastError();
 }
 
-template <typename VT, typename XT, int NC>
-size_t blk_tcheb_smem(const TCsr<VT>& T) {
-  const size_t bytes = (size_t)T.maxU * NC * kBlk * sizeof(XT);
-  if (bytes > 227 * 1024) return 0;
-  // opt in to the shared memory of the largest tile for every MODE instance
-  // (on the current device; called once per context, before any capture)
-  const int lim = (int)std::max<size_t>(bytes, 1);
-  if (cudaFuncSetAttribute(k_tcheb<VT, XT, NC, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
-      cudaFuncSetAttribute(k_tcheb<VT, XT, NC, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
-      cudaFuncSetAttribute(k_tcheb<VT, XT, NC, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess)
-    return 0;
-  return bytes;
-}
-
-template <typename VT, typename XT, int NC>
-void blk_tcheb(const TCsr<VT>& T, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s) {
-  if (T.nrows == 0 || ch.deg == 0) return;
-  const size_t len = (size_t)NC * T.nrows * kBlk;
-  XT* buf[2] = {work, work + len};  // x_j lives in buf[j & 1]
-  const XT it = (XT)ch.inv_theta;
-  const size_t smem = (size_t)T.maxU * NC * kBlk * sizeof(XT);
-  for (int j = 1; j <= ch.deg; ++j) {
-    const XT a = (XT)ch.a[j - 1], c = (XT)ch.c[j - 1];
-    XT* out = j == ch.deg ? x : buf[(j + 1) & 1];
-    const XT* cur = buf[j & 1];
-    const XT* prev = buf[(j + 1) & 1];
-#define NM_TC(MODE)                                                                                             \
-  k_tcheb<VT, XT, NC, MODE><<<T.ntiles, kTT, smem, s>>>(T.nrows, T.R, T.tptr, T.ulist, T.rp, T.li, T.v, b, cur, \
-                                                         prev, out, a, c, it)
-    if (j == 1) NM_TC(0);
-    else if (j == 2) NM_TC(1);
-    else NM_TC(2);
-#undef NM_TC
-    nmg::add_launches(1);
-  }
-}
-template void blk_tcheb<float, float, 3>(const TCsr<float>&, const ChebSetup&, const float*, float*, float*,
-                                         cudaStream_t);
-template void blk_tcheb<float, float, 1>(const TCsr<float>&, const ChebSetup&, const float*, float*, float*,
-                                         cudaStream_t);
-template size_t blk_tcheb_smem<float, float, 3>(const TCsr<float>&);
-template size_t blk_tcheb_smem<float, float, 1>(const TCsr<float>&);
-
 template <typename VT>
 void blk_mass_spmv(const GCsr<VT>& M, const double* x, double* y, cudaStream_t s) {
   k_mass_spmv<VT><<<nrb(M.nrows), kT, 0, s>>>(M.nrows, M.rp, M.ci, M.v, x, y);
@@ -1160,20 +928,6 @@ void blk_ap_cheb_persistent(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b
     return;
   }
   nmg::add_launches(1);
-}
-
-// CTAs of the chunked block kernels: NM_BLK_CTAS_PER_SM (default 8) per SM.
-int blk_grid() {
-  static int g = 0;
-  if (!g) {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int per = 8;
-    if (const char* e = std::getenv("NM_BLK_CTAS_PER_SM")) per = std::max(1, std::atoi(e));
-    g = per * sms;
-  }
-  return g;
 }
 
 int blk_coop_blocks() {

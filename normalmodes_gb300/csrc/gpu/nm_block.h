@@ -37,42 +37,6 @@ struct GCsrHost {
   std::vector<double> v;
 };
 
-// Row-tiled scalar CSR for the shared-memory staged block SpMM.  Rows are
-// cut into tiles of R consecutive rows; ulist[tptr[t] .. tptr[t+1]) holds the
-// distinct columns that tile t touches (ascending) and li[e] the position of
-// entry e's column in that list, so one CTA stages the tile's neighbour rows
-// of the block once in shared memory and every entry then reads shared
-// memory instead of gathering from L2.
-template <typename T>
-struct TCsr {
-  int nrows = 0, R = 0, ntiles = 0, maxU = 0;
-  long long nnz = 0, nu = 0;
-  int* tptr = nullptr;
-  int* ulist = nullptr;
-  int* rp = nullptr;
-  uint16_t* li = nullptr;
-  T* v = nullptr;
-  size_t bytes() const {
-    return (size_t)(ntiles + 1) * 4 + (size_t)nu * 4 + (size_t)(nrows + 1) * 4 + (size_t)nnz * (2 + sizeof(T));
-  }
-};
-struct TCsrHost {
-  int nrows = 0, R = 0, ntiles = 0, maxU = 0;
-  std::vector<int> tptr, ulist, rp;
-  std::vector<uint16_t> li;
-  std::vector<double> v;
-};
-// Tiles of R rows of a scalar grouped CSR (bs == 1); false if a tile would
-// touch more than 65535 distinct columns.
-bool tile_csr(const GCsrHost& g, int R, TCsrHost& t);
-template <typename T>
-int upload_t(nm_ctx* c, const TCsrHost& h, TCsr<T>& d);
-template <typename T>
-void free_t(TCsr<T>& t);
-// Largest R (halving from R0) whose staged tile fits `smem_max` bytes with
-// `row_bytes` per staged row.
-int tile_rows_for(const GCsrHost& g, int R0, size_t row_bytes, size_t smem_max, TCsrHost& t);
-
 // Host extraction from scaled DOF-level CSR; false if the structure is absent.
 bool group_mass(const nm_csr* B, const std::vector<double>& D, GCsrHost& M);
 bool group_bsr3(const nm_csr* A, const std::vector<double>& dl, const std::vector<double>& dr, GCsrHost& G);
@@ -118,14 +82,6 @@ void blk_ap_cheb_persistent(const GCsr<VT>& Ap, const ChebSetup& ch, const XT* b
 template <typename VT, typename XT>
 void blk_amv(const GCsr<VT>& A, const GCsr<VT>* E, const XT* v, const XT* y, XT* out, const XT* vk, const XT* vkm1,
              XT* yacc, const FiltEpi& ep, cudaStream_t s, const GatherCfg& cfg = GatherCfg());
-// Chebyshev solve (three-term form, deg launches) of the block with NC
-// components per row on a tiled matrix: NC = 3 for the mass M (x) I_3,
-// NC = 1 for the pressure matrix Ap.  work holds 2 blocks.
-template <typename VT, typename XT, int NC>
-void blk_tcheb(const TCsr<VT>& T, const ChebSetup& ch, const XT* b, XT* x, XT* work, cudaStream_t s);
-// Shared-memory bytes one CTA of blk_tcheb needs (0 if the tiles do not fit).
-template <typename VT, typename XT, int NC>
-size_t blk_tcheb_smem(const TCsr<VT>& T);
 template <typename VT>
 void blk_mass_spmv(const GCsr<VT>& M, const double* x, double* y, cudaStream_t s);
 // Conversions between basis columns (FP64, column-major chunks) and row-major blocks.
@@ -142,7 +98,6 @@ void blk_f2d_flat(const float* src, double* dst, size_t len, cudaStream_t s);
 template <typename XT>
 void blk_from_colmajor(const double* src, size_t ld, int n, XT* blk, cudaStream_t s);  // blk = src(:, 0:S)^T
 int blk_coop_blocks();
-int blk_grid();
 
 // FP32 copy of a Lanczos basis (chunks of Basis::kChunk columns, ld = n
 // rounded up to 32), the operand of the mixed path's Gram-Schmidt GEMMs.
@@ -179,8 +134,6 @@ struct BlockState {
   bool ok = false;
   GCsr<double> M64, A64, E64, ET64, Ap64;
   GCsr<float> M32, A32, E32, ET32, Ap32;
-  TCsr<float> TM32, TAp32;  // tiled copies for the staged FP32 Chebyshev solves
-  bool tiled = false;
   float* f32 = nullptr;
   double* f64 = nullptr;
   Basis32 V32, Z32;  // FP32 copies of the basis (mixed path)

@@ -78,29 +78,6 @@ int block_build(nm_ctx* c, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, c
         ((rc = upload_g(c, hE, st->E32)) || (rc = upload_g(c, hET, st->ET32)) || (rc = upload_g(c, hAp, st->Ap32))))
       return rc;
   }
-  const char* mk = std::getenv("NM_MASS_KERNEL");
-  const char* ak = std::getenv("NM_AP_KERNEL");
-  if (c->precision == NM_PREC_MIXED && ((mk && std::atoi(mk) == 1) || (ak && std::atoi(ak) == 1))) {
-    // staged FP32 Chebyshev solves (selected with NM_MASS_KERNEL / NM_AP_KERNEL
-    // = 1; measured slower than the gather kernels on GB300): tiles of
-    // consecutive rows whose distinct neighbour rows fit in shared memory
-    // (R halves until they fit)
-    const size_t smem_max = 110 * 1024;
-    int rM = 32, rAp = 32;
-    if (const char* e = std::getenv("NM_TILE_ROWS_M")) rM = std::max(4, std::atoi(e));
-    if (const char* e = std::getenv("NM_TILE_ROWS_AP")) rAp = std::max(4, std::atoi(e));
-    TCsrHost tM, tAp;
-    bool tiled = tile_rows_for(hM, rM, 3 * kBlk * sizeof(float), smem_max, tM) > 0;
-    if (tiled && c->fs) tiled = tile_rows_for(hAp, rAp, kBlk * sizeof(float), smem_max, tAp) > 0;
-    if (tiled) {
-      if ((rc = upload_t(c, tM, st->TM32))) return rc;
-      if (c->fs && (rc = upload_t(c, tAp, st->TAp32))) return rc;
-      tiled = blk_tcheb_smem<float, float, 3>(st->TM32) > 0 &&
-              (!c->fs || blk_tcheb_smem<float, float, 1>(st->TAp32) > 0);
-      cudaGetLastError();
-    }
-    st->tiled = tiled && std::getenv("NM_NO_TILES") == nullptr;
-  }
   blk_prefer_l1();
   st->coop = blk_coop_blocks();
   st->ok = true;
@@ -112,8 +89,6 @@ void block_free(nm_ctx* c) {
   if (!st) return;
   for (auto* g : {&st->M64, &st->A64, &st->E64, &st->ET64, &st->Ap64}) free_g(*g);
   for (auto* g : {&st->M32, &st->A32, &st->E32, &st->ET32, &st->Ap32}) free_g(*g);
-  free_t(st->TM32);
-  free_t(st->TAp32);
   for (float* q : st->V32.chunks) cudaFree(q);
   for (float* q : st->Z32.chunks) cudaFree(q);
   cudaFree(st->f32);
@@ -162,16 +137,6 @@ FiltBufs<XT> filt_carve(XT* base, size_t n, size_t np) {
   return f;
 }
 
-// Kernel choice of the block Chebyshev solves.  0: gather kernel (one row
-// per warp, neighbour rows from L1/L2); 1: staged kernel (tile's neighbour
-// rows copied to shared memory, FP32 only); 2: persistent single-launch
-// kernel (Ap only).  Overridable for measurements with NM_MASS_KERNEL and
-// NM_AP_KERNEL.
-int kernel_choice(const char* env, int dflt) {
-  if (const char* e = std::getenv(env)) return std::atoi(e);
-  return dflt;
-}
-
 // The FP32 filter's inner Chebyshev solves use the degrees of chB32 / chAp32
 // (FP32 accuracy); FP64 solves the reference's degrees.
 template <typename XT>
@@ -194,31 +159,13 @@ const GatherCfg& amv_cfg(nm_ctx* c) {
 template <typename VT, typename XT>
 void blk_mass_solve(nm_ctx* c, const GCsr<VT>& M, const XT* b, XT* x, XT* work) {
   BlockState* st = bs(c);
-  static const int kind = kernel_choice("NM_MASS_KERNEL", 0);
-  if constexpr (std::is_same<XT, float>::value && std::is_same<VT, float>::value) {
-    if (st->tiled && kind == 1) {
-      blk_tcheb<float, float, 3>(st->TM32, mass_cheb<XT>(c), b, x, work, c->stream);
-      return;
-    }
-  }
   blk_mass_cheb<VT, XT>(M, mass_cheb<XT>(c), b, x, work, c->stream,
                         std::is_same<XT, float>::value ? st->gm32 : st->gm64);
 }
 template <typename VT, typename XT>
 void blk_ap_solve(nm_ctx* c, const GCsr<VT>& Ap, const XT* b, XT* x, XT* work) {
   BlockState* st = bs(c);
-  static const int kind = kernel_choice("NM_AP_KERNEL", 0);
-  if constexpr (std::is_same<XT, float>::value && std::is_same<VT, float>::value) {
-    if (st->tiled && kind == 1) {
-      blk_tcheb<float, float, 1>(st->TAp32, ap_cheb<XT>(c), b, x, work, c->stream);
-      return;
-    }
-  }
-  if (kind == 2 && st->coop > 0)  // the persistent kernel reads the reference set-up's device coefficients
-    blk_ap_cheb_persistent<VT, XT>(Ap, c->chebAp, b, x, work, c->bar, c->d_status, st->coop, c->stream);
-  else
-    blk_ap_cheb<VT, XT>(Ap, ap_cheb<XT>(c), b, x, work, c->stream,
-                        std::is_same<XT, float>::value ? st->ga32 : st->ga64);
+  blk_ap_cheb<VT, XT>(Ap, ap_cheb<XT>(c), b, x, work, c->stream, std::is_same<XT, float>::value ? st->ga32 : st->ga64);
 }
 
 
@@ -361,9 +308,7 @@ int block_autotune(nm_ctx* c) {
   BlockState* st = bs(c);
   if (!st || !st->ok || st->tuned) return NM_OK;
   st->tuned = true;
-  if (std::getenv("NM_GATHER_VEC") || std::getenv("NM_GATHER_THREADS")) return NM_OK;  // fixed by hand
-  if (const char* e = std::getenv("NM_AUTOTUNE"))
-    if (std::atoi(e) == 0) return NM_OK;
+  if (c->autotune < 0) return NM_OK;  // nm_opts.autotune: keep the default launch shapes
   const int n = c->n, np = c->np;
   const bool mixed = c->precision == NM_PREC_MIXED;
   const size_t L = (size_t)kBlk * n, P = (size_t)kBlk * (np ? np : 1);
@@ -469,12 +414,13 @@ int block_buffers(nm_ctx* c) {
     CB(c, cublasCreate(&st->cublas));
     CS(c, cusolverDnCreate(&st->cusolver));
   }
-  if (mixed && st->chB32.deg == 0 && std::getenv("NM_FILTER_FULL_DEG") == nullptr) {
-    // FP32 filter: inner Chebyshev solves to FP32 accuracy (2^-24)
+  if (mixed && st->chB32.deg == 0 && c->inner_tol >= 0.0) {
+    // FP32 filter: inner Chebyshev solves to FP32 accuracy (2^-24), or to
+    // nm_opts.inner_tol for the mass solve
     const double eps32 = 5.9604644775390625e-08;
     st->chB32 = c->chebB;
     st->chB32.d_coef = nullptr;
-    st->chB32.deg = cheb_degree_for(c->chebB, eps32);
+    st->chB32.deg = cheb_degree_for(c->chebB, c->inner_tol > 0.0 ? c->inner_tol : eps32);
     cheb_coefs(st->chB32);
     if (c->fs) {
       st->chAp32 = c->chebAp;
@@ -535,9 +481,7 @@ int block_time_op(nm_ctx* c, int which, int reps, double* ms, double* bytes, int
   // x_{j-1} (4)
   auto cheb_streams = [](int deg) { return deg <= 0 ? 0.0 : deg == 1 ? 2.0 : 5.0 + 4.0 * (deg - 2); };
   const double b_mat = (double)nnzM * (vs + 4) + (double)(n / 3 + 1) * 4;
-  // Ap Chebyshev solve: three-term multi-launch form, or the persistent
-  // residual / direction form (6 streams per step)
-  const bool tiled = !(kernel_choice("NM_AP_KERNEL", 0) == 2 && st->coop > 0);
+  // Ap Chebyshev solve: the same three-term multi-launch form
   const double ap_mat = c->fs ? (double)nnzAp * (vs + 4) + (double)(np + 1) * 4 : 0.0;
   const double et = c->fs ? (double)nnzET * (3 * vs + 4) + (double)(np + 1) * 4 + L * xs + P * xs : 0.0;
   const double amv = (double)nnzA * (9 * vs + 4) + (double)(n / 3 + 1) * 4 + (double)nnzE * (3 * vs + 4) +
@@ -570,12 +514,11 @@ int block_time_op(nm_ctx* c, int which, int reps, double* ms, double* bytes, int
     FiltBufs<double> f = filt_carve<double>(st->f64, n, np);
     NM_CUDA(c, cudaMemsetAsync(st->f64, 0, sizeof(double) * filt_len<double>(n, np), c->stream));
     run = [=]() {
-      if (wantB) blk_mass_cheb<double, double>(st->M64, c->chebB, f.vk, f.w2, f.bwork, c->stream);
+      if (wantB) blk_mass_solve<double, double>(c, st->M64, f.vk, f.w2, f.bwork);
       if (wantA) {
         if (c->fs) {
           blk_et<double, double>(st->ET64, f.w2, f.x0, c->stream, st->gA64);
-          blk_ap_cheb_persistent<double, double>(st->Ap64, c->chebAp, f.x0, f.y0, f.apwork, c->bar, c->d_status,
-                                                 st->coop, c->stream);
+          blk_ap_solve<double, double>(c, st->Ap64, f.x0, f.y0, f.apwork);
         }
         blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, f.w2, f.y0, f.vkp1, f.vk, f.vkm1, f.yout, ep,
                                 c->stream, st->gA64);
@@ -587,9 +530,9 @@ int block_time_op(nm_ctx* c, int which, int reps, double* ms, double* bytes, int
     la += dB;
   }
   if (wantA) {
-    const double ap = c->fs ? dAp * ap_mat + (tiled ? cheb_streams(dAp) : 6.0 * dAp) * P * xs : 0.0;
+    const double ap = c->fs ? dAp * ap_mat + cheb_streams(dAp) * P * xs : 0.0;
     by += amv + (c->fs ? et + ap : 0.0);
-    la += c->fs ? (tiled ? 2 + dAp : 3) : 1;
+    la += c->fs ? 2 + dAp : 1;
   }
   for (int i = 0; i < 2; ++i) run();
   cudaEvent_t e0, e1;
@@ -661,7 +604,7 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   double* y064 = carve(p64, Pn);
   double* apw64 = carve(p64, 4 * Pn);
   // mixed path: range form of the filter (FP64 last A-op, p(0) Z added in FP64)
-  const bool range_form = mixed && std::getenv("NM_FILTER_PLAIN") == nullptr;
+  const bool range_form = mixed && c->filter_form == 0;
   const double p0 = filter_at_zero(pol);
   const size_t ldw = n;
   // ---- small device matrices: S x S scratch and H (K x S), T for cuSOLVER
@@ -690,7 +633,7 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   // below what the Lanczos recurrence needs to stay free of ghost copies);
   // W itself, the three-term recurrence, the Cholesky and the basis stay
   // FP64.  The FP64 GEMMs are the fallback when the FP32 copy cannot grow.
-  bool orth32 = mixed && std::getenv("NM_ORTH64") == nullptr;
+  bool orth32 = mixed && c->orth64 == 0;
   float *W32 = nullptr, *T32 = nullptr, *dH32 = nullptr;
   if (orth32) {
     if (cudaMalloc(&W32, sizeof(float) * L) != cudaSuccess || cudaMalloc(&T32, sizeof(float) * L) != cudaSuccess ||

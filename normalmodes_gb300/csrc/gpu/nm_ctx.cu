@@ -164,6 +164,10 @@ int nm_create(nm_ctx** out, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, 
   c->porder = o.porder;
   c->precision = o.precision;
   c->verbose = o.verbose;
+  c->filter_form = o.filter_form;
+  c->orth64 = o.orth64;
+  c->inner_tol = o.inner_tol;
+  c->autotune = o.autotune;
   int rc;
   if ((rc = check_csr(c, B, c->n, c->n, "B"))) return bail(rc);
   if ((rc = check_csr(c, A, c->n, c->n, "A"))) return bail(rc);
