@@ -230,6 +230,14 @@ int nm_kpm_degree(double lmin, double lmax, double lam_lo, double lam_hi, int ns
  * leading dimension ld); runs on the host, so any operator will do. */
 int nm_kpm_moments(nm_block_op op, void* data, int n, double lmin, double lmax, int degree, int nvec,
                    unsigned long long seed, double* mu);
+/* The same moments (same Rademacher vectors and estimator) on the device:
+ * B^-1 A applied to 32-column blocks with the context's block operators (in
+ * FP32 for a mixed-precision context, FP64 otherwise), one on-device dot per
+ * degree and no host round trip until the end.  NM_ERR_ARG if the context has
+ * no block operators (then use nm_kpm_moments with nm_amv_block +
+ * nm_bsolve_block). */
+int nm_kpm_moments_ctx(nm_ctx* ctx, double lmin, double lmax, int degree, int nvec, unsigned long long seed,
+                       double* mu);
 /* Estimated number of eigenvalues in (lam_lo, lam_hi], lam_lo > 0. */
 int nm_kpm_count(const double* mu, int degree, int n, double lmin, double lmax, double lam_lo, double lam_hi,
                  double* count);
@@ -239,7 +247,8 @@ int nm_kpm_count(const double* mu, int degree, int n, double lmin, double lmax, 
 int nm_kpm_slices(const double* mu, int degree, int n, double lmin, double lmax, double f_lo_mhz, double f_hi_mhz,
                   int nslices, nm_slice* out, double* counts);
 /* All of the above on a context: Lanczos bounds (unless given), moments
- * through nm_amv_block + nm_bsolve_block, slices for nm_solve_batched. */
+ * (nm_kpm_moments_ctx, or through nm_amv_block + nm_bsolve_block when the
+ * context has no block operators), slices for nm_solve_batched. */
 int nm_slice_spectrum(nm_ctx* ctx, double f_lo_mhz, double f_hi_mhz, int nslices, const nm_kpm_opts* opts,
                       nm_slice* out, double* counts);
 

@@ -1079,6 +1079,69 @@ __global__ void k_colres_sum(const double* __restrict__ part, int nparts, double
 
 size_t blk_colres_scratch() { return (size_t)kColRedCtas * 2 * kBlk + 2 * kBlk; }
 
+namespace {
+// One KPM step on row-major blocks: W0 <- alpha (T - c W1) - beta W0 (alpha
+// = 2/e, beta = 1 for the three-term step; alpha = 1/e, beta = 0 for T_1),
+// and the per-CTA partial sums of V . W0 (in a fixed order: CTA b sums the
+// grid-stride elements it owns, a tree within the CTA).
+template <typename XT>
+__global__ void __launch_bounds__(256) k_kpm_step(XT* __restrict__ W0, const XT* __restrict__ T,
+                                                  const XT* __restrict__ W1, const XT* __restrict__ V, double c,
+                                                  double alpha, double beta, size_t len, double* __restrict__ part) {
+  __shared__ double red[256];
+  double acc = 0.0;
+  for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < len; i += (size_t)gridDim.x * 256) {
+    const double w = alpha * ((double)T[i] - c * (double)W1[i]) - beta * (double)W0[i];
+    const XT wx = (XT)w;
+    W0[i] = wx;
+    acc = fma((double)V[i], (double)wx, acc);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+template <typename XT>
+__global__ void __launch_bounds__(256) k_vdot_part(const XT* __restrict__ V, const XT* __restrict__ W, size_t len,
+                                                   double* __restrict__ part) {
+  __shared__ double red[256];
+  double acc = 0.0;
+  for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < len; i += (size_t)gridDim.x * 256)
+    acc = fma((double)V[i], (double)W[i], acc);
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+__global__ void k_sum_parts(const double* __restrict__ part, int nparts, double* __restrict__ out) {
+  double s = 0.0;
+  for (int b = 0; b < nparts; ++b) s += part[b];
+  *out = s;
+}
+constexpr int kKpmCtas = 1024;
+}  // namespace
+
+template <typename XT>
+void blk_kpm_step(XT* W0, const XT* T, const XT* W1, const XT* V, double c, double alpha, double beta, size_t len,
+                  double* part, double* out, cudaStream_t s) {
+  const int g = (int)std::max<size_t>(1, std::min<size_t>(kKpmCtas, (len + 255) / 256));
+  if (T) k_kpm_step<XT><<<g, 256, 0, s>>>(W0, T, W1, V, c, alpha, beta, len, part);
+  else k_vdot_part<XT><<<g, 256, 0, s>>>(V, W0, len, part);
+  k_sum_parts<<<1, 1, 0, s>>>(part, g, out);
+  nmg::add_launches(2);
+}
+template void blk_kpm_step<float>(float*, const float*, const float*, const float*, double, double, double, size_t,
+                                  double*, double*, cudaStream_t);
+template void blk_kpm_step<double>(double*, const double*, const double*, const double*, double, double, double,
+                                   size_t, double*, double*, cudaStream_t);
+size_t blk_kpm_scratch() { return kKpmCtas; }
+
 void blk_colres(const double* AU, const double* BU, const double* U, const double* theta, int rows, double* scratch,
                 cudaStream_t s) {
   const int g = std::max(1, std::min(kColRedCtas, (rows + 7) / 8));

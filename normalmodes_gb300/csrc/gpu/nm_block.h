@@ -123,6 +123,20 @@ void blk_force(float* v, const float* R, const float* f, size_t len, cudaStream_
 size_t blk_colres_scratch();
 void blk_colres(const double* AU, const double* BU, const double* U, const double* theta, int rows, double* scratch,
                 cudaStream_t s);
+// KPM moment step over len elements: W0 <- alpha (T - c W1) - beta W0, then
+// *out = V . W0 (double accumulation, fixed summation order; part holds
+// blk_kpm_scratch() doubles).  T == nullptr: only *out = V . W0.
+template <typename XT>
+void blk_kpm_step(XT* W0, const XT* T, const XT* W1, const XT* V, double c, double alpha, double beta, size_t len,
+                  double* part, double* out, cudaStream_t s);
+size_t blk_kpm_scratch();
+// KPM moments mu[0..degree] of the lambda-weighted density of B^-1 A on the
+// device block path (nm_kpm_moments_ctx); nvec Rademacher vectors in blocks
+// of 32, the same vectors and estimator as nm_kpm_moments.
+int kpm_moments_block(nm_ctx* c, double lmin, double lmax, int degree, int nvec, unsigned long long seed,
+                      double* mu);
+// True when the context has no grouped (3-component) block operators.
+bool block_path_missing(nm_ctx* c);
 void blk_add_colmajor(const float* G, const double* sc, int n, double* U, size_t ld, cudaStream_t s);
 // The same on the first ncol columns only (the others of U are not touched).
 void blk_add_colmajor_cols(const float* G, const double* sc, int n, int ncol, double* U, size_t ld, cudaStream_t s);

@@ -1212,6 +1212,105 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
   return NM_OK;
 }
 
+bool block_path_missing(nm_ctx* c) { return !bs(c) || !bs(c)->ok; }
+
+namespace {
+// Y = B~^-1 A X on a row-major block, in the context's block precision
+// (A-operator, then the mass Chebyshev solve: the order of nm_kpm_moments'
+// callback).
+template <typename XT>
+void kpm_apply(nm_ctx* c, FiltBufs<XT>& f, const XT* X, XT* Y) {
+  BlockState* st = bs(c);
+  cudaStream_t s = c->stream;
+  FiltEpi ep0;  // plain product
+  if constexpr (std::is_same<XT, float>::value) {
+    if (c->fs) {
+      blk_et<float, float>(st->ET32, X, f.x0, s, st->gA32);
+      blk_ap_solve<float, float>(c, st->Ap32, f.x0, f.y0, f.apwork);
+    }
+    blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, X, f.y0, f.w2, nullptr, nullptr, nullptr, ep0, s,
+                          st->gA32);
+    blk_mass_solve<float, float>(c, st->M32, f.w2, Y, f.bwork);
+  } else {
+    if (c->fs) {
+      blk_et<double, double>(st->ET64, X, f.x0, s, st->gA64);
+      blk_ap_solve<double, double>(c, st->Ap64, f.x0, f.y0, f.apwork);
+    }
+    blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, X, f.y0, f.w2, nullptr, nullptr, nullptr, ep0, s,
+                            st->gA64);
+    blk_mass_solve<double, double>(c, st->M64, f.w2, Y, f.bwork);
+  }
+  ++c->n_amv;
+}
+
+template <typename XT>
+int kpm_moments_t(nm_ctx* c, XT* base, double lmin, double lmax, int degree, int nvec, unsigned long long seed,
+                  double* mu) {
+  const int n = c->n, np = c->np, S = kBlk;
+  cudaStream_t s = c->stream;
+  const size_t L = (size_t)S * n;
+  FiltBufs<XT> f = filt_carve<XT>(base, n, np);
+  XT* V = f.zin;
+  XT *W0 = f.vk, *W1 = f.vkm1, *T = f.vkp1;
+  const double cc = 0.5 * (lmax + lmin), e = 0.5 * (lmax - lmin);
+  double *dmu = nullptr, *dpart = nullptr;
+  auto release = [&]() {
+    cudaStreamSynchronize(s);
+    cudaFree(dmu);
+    cudaFree(dpart);
+    dmu = dpart = nullptr;
+  };
+  auto guard = on_exit(release);
+  if (cudaMalloc(&dmu, sizeof(double) * (degree + 1)) != cudaSuccess ||
+      cudaMalloc(&dpart, sizeof(double) * blk_kpm_scratch()) != cudaSuccess) {
+    release();
+    return set_err(c, NM_ERR_OOM, "KPM workspace");
+  }
+  std::vector<double> sum(degree + 1, 0.0), hmu(degree + 1);
+  std::vector<XT> hv(L);
+  for (int j0 = 0; j0 < nvec; j0 += S) {
+    // the same Rademacher vectors as nm_kpm_moments, columns j0 .. j0+31
+    // (zero past nvec: a zero column adds nothing to the moments)
+    for (int i = 0; i < n; ++i)
+      for (int jj = 0; jj < S; ++jj)
+        hv[(size_t)i * S + jj] = j0 + jj < nvec ? (XT)rademacher(seed, j0 + jj, n, i) : (XT)0;
+    NM_CUDA(c, cudaMemcpyAsync(V, hv.data(), sizeof(XT) * L, cudaMemcpyHostToDevice, s));
+    kpm_apply<XT>(c, f, V, W0);  // T_0(S) B^-1 A V
+    blk_kpm_step<XT>(W0, nullptr, nullptr, V, 0.0, 0.0, 0.0, L, dpart, dmu, s);
+    if (degree >= 1) {
+      kpm_apply<XT>(c, f, W0, T);  // W1 = (T - c W0) / e
+      NM_CUDA(c, cudaMemsetAsync(W1, 0, sizeof(XT) * L, s));
+      blk_kpm_step<XT>(W1, T, W0, V, cc, 1.0 / e, 0.0, L, dpart, dmu + 1, s);
+    }
+    for (int k = 2; k <= degree; ++k) {
+      kpm_apply<XT>(c, f, W1, T);  // W0 <- 2 (T - c W1) / e - W0, then swap
+      blk_kpm_step<XT>(W0, T, W1, V, cc, 2.0 / e, 1.0, L, dpart, dmu + k, s);
+      std::swap(W0, W1);
+      if (c->progress && k % 64 == 0) progress(c, NM_PHASE_LANCZOS, k, degree);
+    }
+    NM_CUDA(c, cudaMemcpyAsync(hmu.data(), dmu, sizeof(double) * (degree + 1), cudaMemcpyDeviceToHost, s));
+    NM_CUDA(c, cudaStreamSynchronize(s));
+    NM_CUDA(c, cudaGetLastError());
+    for (int k = 0; k <= degree; ++k) sum[k] += hmu[k];
+  }
+  int rc;
+  if ((rc = check_status(c))) return rc;
+  for (int k = 0; k <= degree; ++k) mu[k] = sum[k] / ((double)n * nvec);
+  return NM_OK;
+}
+}  // namespace
+
+int kpm_moments_block(nm_ctx* c, double lmin, double lmax, int degree, int nvec, unsigned long long seed,
+                      double* mu) {
+  if (block_path_missing(c)) return set_err(c, NM_ERR_ARG, "the device KPM moments need the block operators");
+  if (!(lmax > lmin) || degree < 1 || nvec < 1 || !mu) return set_err(c, NM_ERR_ARG, "KPM: bad arguments");
+  int rc;
+  if ((rc = block_buffers(c))) return rc;
+  BlockState* st = bs(c);
+  return c->precision == NM_PREC_MIXED ? kpm_moments_t<float>(c, st->f32, lmin, lmax, degree, nvec, seed, mu)
+                                       : kpm_moments_t<double>(c, st->f64, lmin, lmax, degree, nvec, seed, mu);
+}
+
 int refine_block_degree(const std::vector<double>& theta, const std::vector<double>& res2, double c0, double lmax,
                         const RefineParams& rp) {
   double need = 0.0;
@@ -1362,6 +1461,11 @@ int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
 
 // ---------------------------------------------------------------- test hooks
 extern "C" {
+int nm_kpm_moments_ctx(nm_ctx* c, double lmin, double lmax, int degree, int nvec, unsigned long long seed,
+                       double* mu) {
+  if (!c) return NM_ERR_ARG;
+  return nmg::kpm_moments_block(c, lmin, lmax, degree, nvec, seed, mu);
+}
 int nm_test_cheb_degree(double lmin, double lmax, int ref_deg, double eps) {
   nmg::ChebSetup ch;
   ch.lmin = lmin;

@@ -138,6 +138,18 @@ inline void progress(nm_ctx* c, int phase, int done, int total) {
   c->progress(c->progress_data, phase, done, total);
 }
 
+// Entry (i, j) of the j-th Rademacher vector of length n for the KPM
+// moments (+1 or -1 from splitmix64 of a per-entry counter): the host and
+// the device moment routines use the same vectors.
+inline double rademacher(unsigned long long seed, int j, int n, int i) {
+  uint64_t x = seed * 0x100000001B3ull + (uint64_t)j * (uint64_t)n + (uint64_t)i;
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  x ^= x >> 31;
+  return (x >> 63) ? 1.0 : -1.0;
+}
+
 // Runs f when the scope ends (device scratch released on every return path).
 template <typename F>
 struct OnExit {

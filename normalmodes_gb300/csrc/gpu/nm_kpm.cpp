@@ -21,16 +21,18 @@
 // eigenvalues carry zero weight whatever the polynomial does at 0.  The
 // slicer then cuts [a, b] at equal counts.
 //
-// The moment recurrence is host code over a block-operator callback (as
-// pEVSL takes its matvecs through registered callbacks), so it runs on the
-// CPU against any operator; nm_slice_spectrum binds it to a context's
-// A-operator and B-solve.
+// nm_kpm_moments is host code over a block-operator callback (as pEVSL takes
+// its matvecs through registered callbacks), so it runs on the CPU against
+// any operator; nm_kpm_moments_ctx (nm_blocksolve.cu) runs the same estimator
+// on the device block operators, and nm_slice_spectrum uses it whenever the
+// context has them.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <vector>
 
+#include "nm_block.h"
 #include "nm_internal.h"
 #include "nm_ops.h"
 
@@ -42,13 +44,6 @@ std::vector<double> jackson(int m) {
   const double th = M_PI / (m + 2);
   for (int k = 0; k <= m; ++k) g[k] = ((m + 2 - k) * std::cos(k * th) + std::sin(k * th) / std::tan(th)) / (m + 2);
   return g;
-}
-
-inline uint64_t mix64(uint64_t x) {
-  x += 0x9E3779B97F4A7C15ull;
-  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
-  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
-  return x ^ (x >> 31);
 }
 
 // The single-precision PI literal and REAL(4) frequencies of the reference's
@@ -140,8 +135,7 @@ int nm_kpm_moments(nm_block_op op, void* data, int n, double lmin, double lmax, 
   const size_t len = (size_t)n * nvec;
   std::vector<double> V(len), W0(len), W1(len), T(len);
   for (int j = 0; j < nvec; ++j)
-    for (int i = 0; i < n; ++i)
-      V[(size_t)j * n + i] = (mix64(seed * 0x100000001B3ull + (uint64_t)j * (uint64_t)n + (uint64_t)i) >> 63) ? 1.0 : -1.0;
+    for (int i = 0; i < n; ++i) V[(size_t)j * n + i] = nmg::rademacher(seed, j, n, i);
   // v'w as partial sums over fixed chunks added in order: the moments, and
   // with them the slices, do not depend on the thread count.
   constexpr long long kChunk = 1 << 16;
@@ -246,8 +240,14 @@ int nm_slice_spectrum(nm_ctx* c, double f_lo_mhz, double f_hi_mhz, int nslices, 
                                : nm_kpm_degree(lmin, lmax, lam_of_f(f_lo_mhz), lam_of_f(f_hi_mhz), nslices);
   const int nvec = o.nvec > 0 ? o.nvec : 16;
   std::vector<double> mu(deg + 1);
-  CtxOp data{c, std::vector<double>((size_t)c->n * nvec)};
-  if ((rc = nm_kpm_moments(ctx_op, &data, c->n, lmin, lmax, deg, nvec, o.seed, mu.data()))) return rc;
+  // moments on the device block path when the context has it (no host
+  // round trip per degree), else through the host block callbacks
+  rc = nm_kpm_moments_ctx(c, lmin, lmax, deg, nvec, o.seed, mu.data());
+  if (rc == NM_ERR_ARG && nmg::block_path_missing(c)) {
+    CtxOp data{c, std::vector<double>((size_t)c->n * nvec)};
+    rc = nm_kpm_moments(ctx_op, &data, c->n, lmin, lmax, deg, nvec, o.seed, mu.data());
+  }
+  if (rc) return rc;
   if ((rc = nm_kpm_slices(mu.data(), deg, c->n, lmin, lmax, f_lo_mhz, f_hi_mhz, nslices, out, counts)))
     return nmg::set_err(c, rc, "slicing failed");
   return NM_OK;

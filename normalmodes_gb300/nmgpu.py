@@ -212,6 +212,7 @@ def lib() -> C.CDLL:
         L.nm_kpm_degree.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
         L.nm_kpm_moments.argtypes = [NM_BLOCK_OP, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
                                      C.c_ulonglong, dp]
+        L.nm_kpm_moments_ctx.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_ulonglong, dp]
         L.nm_kpm_count.argtypes = [dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, dp]
         L.nm_kpm_slices.argtypes = [dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
                                     C.POINTER(NmSlice), dp]
@@ -420,6 +421,13 @@ class Solver:
         finally:
             for i in range(len(slices)):
                 L.nm_result_free(C.byref(res[i]))
+
+    def kpm_moments(self, lmin: float, lmax: float, degree: int, nvec: int = 16, seed: int = 0x4B504D):
+        """nm_kpm_moments_ctx: the KPM moments mu[0..degree] of the
+        lambda-weighted density of B^-1 A on the device block operators."""
+        mu = np.zeros(degree + 1)
+        self._check(lib().nm_kpm_moments_ctx(self._h, lmin, lmax, degree, nvec, seed, _dp(mu)))
+        return mu
 
     def slice_spectrum(self, lowfreq: float, upfreq: float, nslices: int, degree: int = 0, nvec: int = 16,
                        seed: int = 0x4B504D, ab_bounds=None):
