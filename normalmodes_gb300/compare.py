@@ -30,6 +30,13 @@ def main(argv=None) -> None:
     ap.add_argument("--fp64-lam", default=None, help="eigenvalues of an earlier FP64 solve (.npy) instead of solving")
     ap.add_argument("--save-fp64-lam", default=None, help="write the FP64 eigenvalues to this .npy file")
     ap.add_argument("--gravity", action="store_true", help="operators with the reference gravity (JOB = 2)")
+    ap.add_argument("--inner-tol", type=float, default=0.0,
+                    help="mixed path: accuracy of the FP32 filter's inner B^-1 solve (0: 2^-24)")
+    ap.add_argument("--resid-tol", type=float, default=0.0, help="mixed path: refinement target err_ref (0: 1e-10)")
+    ap.add_argument("--refine-sweeps", type=int, default=0)
+    ap.add_argument("--refine-maxdeg", type=int, default=0)
+    ap.add_argument("--skip-fp64", action="store_true", help="mixed path only (no comparison)")
+    ap.add_argument("--verbose", action="store_true")
     a = ap.parse_args(argv)
     from normalmodes_gb300.model import Model
     from normalmodes_gb300.nmgpu import NM_PREC_FP64, NM_PREC_MIXED, Solver
@@ -39,13 +46,17 @@ def main(argv=None) -> None:
     mats = Model.ball(gravity=a.gravity, **kw).operators()
     lo, hi = a.interval
     out = {"cells": a.cells, "porder": a.porder, "lateral": a.lateral, "interval_mhz": [lo, hi], "polish": a.polish,
-           "gravity": a.gravity}
+           "gravity": a.gravity, "inner_tol": a.inner_tol, "resid_tol": a.resid_tol,
+           "refine_sweeps": a.refine_sweeps, "refine_maxdeg": a.refine_maxdeg}
     res = {}
-    runs = [("mixed", NM_PREC_MIXED, 32)] + ([] if a.fp64_lam else [("fp64", NM_PREC_FP64, a.fp64_block)])
+    runs = [("mixed", NM_PREC_MIXED, 32)] + ([] if (a.fp64_lam or a.skip_fp64) else
+                                              [("fp64", NM_PREC_FP64, a.fp64_block)])
     for name, prec, block in runs:
-        with Solver(mats, a.porder, precision=prec) as sv:
+        with Solver(mats, a.porder, precision=prec, inner_tol=a.inner_tol, verbose=a.verbose) as sv:
             t = time.perf_counter()
-            r = sv.solve(lo, hi, block=block, want_vectors=False, polish=a.polish if name == "mixed" else 0)
+            kw = dict(polish=a.polish, resid_tol=a.resid_tol, refine_sweeps=a.refine_sweeps,
+                      refine_maxdeg=a.refine_maxdeg) if name == "mixed" else {}
+            r = sv.solve(lo, hi, block=block, want_vectors=False, **kw)
             dt = time.perf_counter() - t
         res[name] = r
         out[name] = {"nev": len(r.lam), "seconds": round(dt, 3), "block": block, "lanczos_vectors": r.lanczos_steps,
@@ -58,6 +69,9 @@ def main(argv=None) -> None:
                      "refinement": {k: r.counts[k] for k in ("refine_passes", "refine_blocks", "refine_maxdeg",
                                                              "refine_steps", "res2_before_refine")}}
     m = res["mixed"].lam
+    if a.skip_fp64 and not a.fp64_lam:
+        print(json.dumps(out))
+        return
     f = np.load(a.fp64_lam) if a.fp64_lam else res["fp64"].lam
     if a.save_fp64_lam and "fp64" in res:
         np.save(a.save_fp64_lam, f)

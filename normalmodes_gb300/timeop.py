@@ -26,6 +26,9 @@ def main(argv=None) -> None:
     ap.add_argument("--ops", default="4,5,6")
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--gravity", action="store_true", help="operators with the reference gravity (JOB = 2)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--verbose", action="store_true", help="print every autotuner candidate's time")
+    ap.add_argument("--inner-tol", type=float, default=0.0, help="accuracy of the FP32 inner B^-1 solve")
     a = ap.parse_args(argv)
     from normalmodes_gb300.model import Model
     from normalmodes_gb300.nmgpu import NM_PREC_FP64, NM_PREC_MIXED, Solver
@@ -36,7 +39,8 @@ def main(argv=None) -> None:
     m = Model.ball(gravity=a.gravity, **kw)
     mats = m.operators()
     t_model = time.perf_counter() - t
-    with Solver(mats, a.porder, precision=NM_PREC_MIXED if a.precision == "mixed" else NM_PREC_FP64) as sv:
+    with Solver(mats, a.porder, precision=NM_PREC_MIXED if a.precision == "mixed" else NM_PREC_FP64,
+                autotune=-1 if a.no_autotune else 0, verbose=a.verbose, inner_tol=a.inner_tol) as sv:
         info = sv.info()
         out = {"cells": a.cells, "porder": a.porder, "n": info.n, "np": info.np, "precision": a.precision,
                "model_s": round(t_model, 2)}
@@ -45,8 +49,9 @@ def main(argv=None) -> None:
             out[str(w)] = {"ms": round(ms, 4), "GBs": round(by / ms / 1e6, 1), "launches": la,
                            "bytes": by}
         i2 = sv.info()
-        out["autotuned"] = {"mass_vec": i2.mass_vec, "mass_threads": i2.mass_threads, "ap_vec": i2.ap_vec,
-                            "ap_threads": i2.ap_threads}
+        out["autotuned"] = {"mass_vec": i2.mass_vec, "mass_threads": i2.mass_threads, "mass_sweep": i2.mass_sweep,
+                            "ap_vec": i2.ap_vec, "ap_threads": i2.ap_threads, "ap_sweep": i2.ap_sweep,
+                            "aop_threads": i2.aop_threads, "aop_sweep": i2.aop_sweep}
     print(json.dumps(out))
 
 
