@@ -110,6 +110,8 @@ typedef struct {
   int refine_sweeps;  /* adaptive refinement: at most this many passes, each
                          closed by an FP64 Rayleigh-Ritz (0: 2)                 */
   int refine_maxdeg;  /* adaptive refinement: degree cap per block (0: 4000)      */
+  double refine_band; /* adaptive refinement: the damped band starts at this
+                         multiple of the block's largest Ritz value (0: 5)     */
   nm_progress_fn progress; /* host callback at phase boundaries (NULL: none)      */
   void* progress_data;     /* first argument of progress                          */
 } nm_solve_opts;

@@ -41,6 +41,7 @@ module nmgpu_mod
     integer(c_int) :: damping, want_vectors, unscale, use_graph, block, polish
     real(c_double) :: resid_tol
     integer(c_int) :: refine_sweeps, refine_maxdeg
+    real(c_double) :: refine_band
     type(c_funptr) :: progress
     type(c_ptr) :: progress_data
   end type nm_solve_opts

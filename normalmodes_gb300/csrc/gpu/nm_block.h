@@ -217,20 +217,33 @@ double filter_at_zero(const Pol& pol);
 // in FP32 (it is small, so FP32 rounding stays at FP64 level relative to U).
 int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, const PolishPlan& plan);
 
-// Adaptive refinement of the mixed path (polish = 0), the same correction
-// U <- U + B~^-1 D / T_d(l(theta)) as polish64 driven by the FP64 residual
-// R = A U - theta B U, with the band and degree chosen per block of 32 Ritz
-// vectors from R itself: the band [c, lmax] starts at c = band * (largest
-// theta of the block), and the degree is the smallest that damps every
-// column's residual below tol_res2 with a margin `safety`:
-//   d = max_j acosh(safety res2_j / tol_res2) / acosh(1 + 2 (c - theta_j) / (lmax - c)),
+// Adaptive refinement of the mixed path (polish = 0): U <- h(B~^-1 A) U per
+// Ritz vector with
+//   h(x) = (x / theta) T_d(l(x)) / T_d(l(theta)),  l: [c, lmax] -> [-1, 1],
+// applied in correction form, both factors driven by FP64 residuals
+// R = A U - theta B U and computed in FP32 (the corrections are small, so
+// their FP32 rounding stays far below FP64 level relative to U):
+//  * T_d(l(.)) / T_d(l(theta)) damps the band [c, lmax], where FP32 rounding
+//    of the filter left components of relative size ~1e-7 that the residual
+//    weighs by lambda / theta (up to 1e6 for the lowest modes);
+//  * x / theta (one step U + B~^-1 R / theta, "purge") is zero on the null
+//    space of A, the zero-frequency fluid modes, whose FP32-level content no
+//    polynomial normalised at theta can damp.
+// Any polynomial normalised at theta grows below it: with the band starting
+// at c = band * (largest theta of the block), band = 5, the growth of the
+// lower modes is about D^0.12 for a damping D, and the Rayleigh-Ritz over
+// all Ritz vectors that closes each pass removes it along the other wanted
+// modes.  The degree per block of 32 Ritz vectors is the smallest that
+// brings every column's residual below tol_res2 with a margin `safety`,
+// including the factor lmax / theta the purge multiplies the band by:
+//   d = max_j acosh(safety (lmax/theta_j) res2_j / tol_res2)
+//             / acosh(1 + 2 (c - theta_j) / (lmax - c)),
 // clamped to [mindeg, maxdeg]; blocks already below tol_res2 are left alone.
-// Components along modes below c are not damped; the FP64 Rayleigh-Ritz
-// that follows each pass removes those along the other Ritz vectors.
 struct RefineParams {
   double tol_res2 = 1e-7;  // target ||A u - theta B u||_2 / (|theta| ||u||_B)
-  double band = 2.0;
+  double band = 5.0;
   double safety = 4.0;
+  bool purge = true;
   int mindeg = 8, maxdeg = 4000;
 };
 struct RefineStats {

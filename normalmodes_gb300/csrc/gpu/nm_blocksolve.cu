@@ -1315,8 +1315,10 @@ int refine_block_degree(const std::vector<double>& theta, const std::vector<doub
                         const RefineParams& rp) {
   double need = 0.0;
   for (size_t j = 0; j < theta.size() && j < res2.size(); ++j) {
-    const double damp = rp.safety * res2[j] / rp.tol_res2;
-    if (!(damp > 1.0)) continue;
+    if (!(res2[j] > rp.tol_res2) || !(theta[j] > 0.0)) continue;
+    // the closing (B~^-1 A) / theta step multiplies the band's components by
+    // up to lmax / theta: the damping has to cover that too
+    const double damp = rp.safety * (rp.purge ? lmax / theta[j] : 1.0) * res2[j] / rp.tol_res2;
     const double delta = 2.0 * (c0 - theta[j]) / (lmax - c0);
     if (!(delta > 0.0)) continue;  // at or above the band: not refinable
     need = std::max(need, std::acosh(damp) / std::acosh(1.0 + delta));
@@ -1444,6 +1446,27 @@ int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
       // U += B~^-1 D_deg / T_deg(l(theta))
       blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
       blk_add_colmajor_cols(f.w2, dsc, n, ncol, U + (size_t)j0 * n, n, s);
+      if (rp.purge) {
+        // U <- (B~^-1 A / theta) U = U + B~^-1 (A U - theta B U) / theta: exactly
+        // zero on the null space of A (the zero-frequency fluid modes, whose
+        // FP32-level content the Gram-Schmidt and Ritz products leave in U),
+        // up to the accuracy of B~^-1 B; the residual is FP64 and small, so the
+        // FP32 solve adds rounding far below FP64 level relative to U
+        blk_from_colmajor_cols(U + (size_t)j0 * n, n, n, ncol, sin_, s);
+        if (c->fs) {
+          blk_et<double, double>(st->ET64, sin_, x0, s, st->gA64);
+          blk_ap_solve<double, double>(c, st->Ap64, x0, y0, apw);
+        }
+        blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sAU, nullptr, nullptr, nullptr, ep0, s,
+                                st->gA64);
+        blk_mass_spmv<double>(st->M64, sin_, sBU, s);
+        blk_resid_f32(sAU, sBU, dth, f.zin, 1.0f, L, s);
+        blk_mass_solve<float, float>(c, st->M32, f.zin, f.w2, f.bwork);
+        for (int col = 0; col < S; ++col) sc[col] = col < ncol && th[col] > 0.0 ? 1.0 / th[col] : 0.0;
+        NM_CUDA(c, cudaMemcpyAsync(dsc, sc.data(), sizeof(double) * S, cudaMemcpyHostToDevice, s));
+        blk_add_colmajor_cols(f.w2, dsc, n, ncol, U + (size_t)j0 * n, n, s);
+        ++c->n_amv;
+      }
       c->n_amv += (long long)deg * S;
       stats.blocks += 1;
       stats.steps += deg;

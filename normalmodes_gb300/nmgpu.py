@@ -51,7 +51,8 @@ class NmSolveOpts(C.Structure):
                 ("mlan_bounds", C.c_int), ("ab_bounds", C.c_double * 2), ("damping", C.c_int),
                 ("want_vectors", C.c_int), ("unscale", C.c_int), ("use_graph", C.c_int), ("block", C.c_int),
                 ("polish", C.c_int), ("resid_tol", C.c_double), ("refine_sweeps", C.c_int),
-                ("refine_maxdeg", C.c_int), ("progress", C.c_void_p), ("progress_data", C.c_void_p)]
+                ("refine_maxdeg", C.c_int), ("refine_band", C.c_double), ("progress", C.c_void_p),
+                ("progress_data", C.c_void_p)]
 
 
 # void (*)(void* data, int phase, int done, int total)
@@ -344,12 +345,13 @@ class Solver:
     @staticmethod
     def _solve_opts(maxit=0, tol=0.0, ab_bounds=None, want_vectors=True, unscale=False, use_graph=True, damping=1,
                     mlan_bounds=0, block=0, polish=0, resid_tol=0.0, refine_sweeps=0, refine_maxdeg=0,
-                    progress=None) -> "NmSolveOpts":
+                    progress=None, refine_band=0.0) -> "NmSolveOpts":
         o = NmSolveOpts()
         lib().nm_default_solve_opts(C.byref(o))
         o.resid_tol = resid_tol
         o.refine_sweeps = refine_sweeps
         o.refine_maxdeg = refine_maxdeg
+        o.refine_band = refine_band
         if progress is not None:  # an NM_PROGRESS_FN the caller keeps alive for the call
             o.progress = C.cast(progress, C.c_void_p)
         o.maxit = maxit
@@ -386,7 +388,7 @@ class Solver:
               want_vectors: bool = True, unscale: bool = False, use_graph: bool = True, damping: int = 1,
               mlan_bounds: int = 0, allow_noconv: bool = False, block: int = 0, polish: int = 0,
               resid_tol: float = 0.0, refine_sweeps: int = 0, refine_maxdeg: int = 0,
-              progress=None) -> SolveResult:
+              progress=None, refine_band: float = 0.0) -> SolveResult:
         """nm_solve on [lowfreq, upfreq] mHz.  `progress`, if given, is a
         Python callable progress(phase, done, total) called at the solve's
         phase and block boundaries (NM_PHASE_*), stream drained."""
@@ -395,7 +397,7 @@ class Solver:
         if progress is not None:
             cb = NM_PROGRESS_FN(lambda _d, ph, done, tot: progress(ph, done, tot))
         o = self._solve_opts(maxit, tol, ab_bounds, want_vectors, unscale, use_graph, damping, mlan_bounds, block,
-                             polish, resid_tol, refine_sweeps, refine_maxdeg, cb)
+                             polish, resid_tol, refine_sweeps, refine_maxdeg, cb, refine_band)
         r = NmResult()
         rc = L.nm_solve(self._h, lowfreq, upfreq, C.byref(o), C.byref(r))
         try:
