@@ -1484,6 +1484,24 @@ int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
 
 // ---------------------------------------------------------------- test hooks
 extern "C" {
+// Pins the launch shape of one family of block gather kernels (kind 0 mass,
+// 1 Ap, 2 A-op; in the context's precision) and marks the context tuned, so
+// a profile captures that shape without the autotuner's trial launches.
+int nm_test_gather_shape(nm_ctx* c, int kind, int vec, int threads, int sweep) {
+  if (!c || !c->blk || kind < 0 || kind > 2) return NM_ERR_ARG;
+  nmg::BlockState* st = (nmg::BlockState*)c->blk;
+  const bool mixed = c->precision == NM_PREC_MIXED;
+  nmg::GatherCfg g;
+  g.vec = vec;
+  g.threads = threads;
+  g.sweep = sweep;
+  nmg::GatherCfg* t = kind == 0 ? (mixed ? &st->gm32 : &st->gm64)
+                      : kind == 1 ? (mixed ? &st->ga32 : &st->ga64) : (mixed ? &st->gA32 : &st->gA64);
+  *t = g;
+  st->tuned = true;
+  return NM_OK;
+}
+
 int nm_kpm_moments_ctx(nm_ctx* c, double lmin, double lmax, int degree, int nvec, unsigned long long seed,
                        double* mu) {
   if (!c) return NM_ERR_ARG;

@@ -214,6 +214,7 @@ def lib() -> C.CDLL:
         L.nm_kpm_moments.argtypes = [NM_BLOCK_OP, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
                                      C.c_ulonglong, dp]
         L.nm_kpm_moments_ctx.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_ulonglong, dp]
+        L.nm_test_gather_shape.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
         L.nm_kpm_count.argtypes = [dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, dp]
         L.nm_kpm_slices.argtypes = [dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
                                     C.POINTER(NmSlice), dp]

@@ -29,6 +29,9 @@ def main(argv=None) -> None:
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--verbose", action="store_true", help="print every autotuner candidate's time")
     ap.add_argument("--inner-tol", type=float, default=0.0, help="accuracy of the FP32 inner B^-1 solve")
+    ap.add_argument("--shape", action="append", default=[],
+                    help="pin a launch shape instead of autotuning: KIND:VEC,THREADS,SWEEP with KIND mass|ap|aop "
+                         "(e.g. mass:0,1024,1); repeatable")
     a = ap.parse_args(argv)
     from normalmodes_gb300.model import Model
     from normalmodes_gb300.nmgpu import NM_PREC_FP64, NM_PREC_MIXED, Solver
@@ -41,6 +44,13 @@ def main(argv=None) -> None:
     t_model = time.perf_counter() - t
     with Solver(mats, a.porder, precision=NM_PREC_MIXED if a.precision == "mixed" else NM_PREC_FP64,
                 autotune=-1 if a.no_autotune else 0, verbose=a.verbose, inner_tol=a.inner_tol) as sv:
+        if a.shape:
+            from normalmodes_gb300.nmgpu import lib
+            kinds = {"mass": 0, "ap": 1, "aop": 2}
+            for spec in a.shape:  # before the first block use, so the autotuner does not run
+                k, v = spec.split(":")
+                vec, thr, sw = (int(x) for x in v.split(","))
+                sv._check(lib().nm_test_gather_shape(sv._h, kinds[k], vec, thr, sw))
         info = sv.info()
         out = {"cells": a.cells, "porder": a.porder, "n": info.n, "np": info.np, "precision": a.precision,
                "model_s": round(t_model, 2)}
