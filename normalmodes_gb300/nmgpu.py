@@ -215,6 +215,7 @@ def lib() -> C.CDLL:
                                      C.c_ulonglong, dp]
         L.nm_kpm_moments_ctx.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_ulonglong, dp]
         L.nm_test_gather_shape.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.nm_test_gs_tc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int]
         L.nm_kpm_count.argtypes = [dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, dp]
         L.nm_kpm_slices.argtypes = [dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
                                     C.POINTER(NmSlice), dp]
