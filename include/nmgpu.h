@@ -64,7 +64,10 @@ typedef struct {
   int filter_form;   /* 0: range form W = p(0) Z + A B~^-1 Y (last A-op in FP64,
                         no FP32 rounding in the zero-frequency modes); 1: the
                         plain FP32 filter                                        */
-  int orth64;        /* 1: FP64 block Gram-Schmidt (0: FP32 on FP32 basis copies) */
+  int orth;          /* block Gram-Schmidt of the mixed path against the FP32
+                        basis copies: 0 the projection V^T W on the tensor cores
+                        (tcgen05, 3xTF32) where the GPU has them, else cuBLAS
+                        SGEMM; 1 FP64 (DGEMM on the FP64 basis); 2 SGEMM     */
   double inner_tol;  /* relative accuracy of the FP32 filter's inner B~^-1
                         Chebyshev solve, which sets its degree (0: 2^-24, FP32;
                         < 0: the reference's degree)                           */

@@ -28,7 +28,7 @@ module nmgpu_mod
     integer(c_int) :: porder, device, b_cheb_deg, ap_cheb_deg
     real(c_double) :: b_bounds(2), ap_bounds(2)
     integer(c_int) :: precision, verbose
-    integer(c_int) :: filter_form, orth64
+    integer(c_int) :: filter_form, orth
     real(c_double) :: inner_tol
     integer(c_int) :: autotune
   end type nm_opts

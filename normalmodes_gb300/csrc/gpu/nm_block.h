@@ -137,6 +137,21 @@ int kpm_moments_block(nm_ctx* c, double lmin, double lmax, int degree, int nvec,
                       double* mu);
 // True when the context has no grouped (3-component) block operators.
 bool block_path_missing(nm_ctx* c);
+
+// Tensor-core Gram-Schmidt projection (nm_gs_tc.cu): H = V^T W for the FP32
+// basis copy V (n x K, K a multiple of 32, chunks of 64 columns) and a
+// 32-column FP32 block W, on tcgen05 (kind::tf32, 3xTF32 split).
+// gs_tc_map encodes the TMA descriptor (CUtensorMap, gs_tc_map_bytes()
+// bytes) of one 64-column chunk or of W (cols 32); base 16-byte aligned,
+// ld a multiple of 4.  part holds gs_tc_part_floats(K, n) floats; status
+// gets 2 if a bounded wait of the kernel ran out.  H is column-major with
+// leading dimension ldh.
+bool gs_tc_available();
+size_t gs_tc_map_bytes();
+int gs_tc_map(const float* base, int n, size_t ld, int cols, void* map_out);
+size_t gs_tc_part_floats(int K, int n);
+int gs_tc_project(const void* vmaps_dev, const void* wmap_dev, int K, int n, float* part, float* H, int ldh,
+                  int* status, cudaStream_t s);
 void blk_add_colmajor(const float* G, const double* sc, int n, double* U, size_t ld, cudaStream_t s);
 // The same on the first ncol columns only (the others of U are not touched).
 void blk_add_colmajor_cols(const float* G, const double* sc, int n, int ncol, double* U, size_t ld, cudaStream_t s);
@@ -151,6 +166,11 @@ struct BlockState {
   float* f32 = nullptr;
   double* f64 = nullptr;
   Basis32 V32, Z32;  // FP32 copies of the basis (mixed path)
+  // TMA descriptors of the V32 chunks for the tensor-core projection
+  // (host copies, 64-byte aligned, and their device array)
+  std::vector<uint8_t> vmaps;
+  int vmaps_n = 0;
+  void* d_vmaps = nullptr;
   // Chebyshev set-ups of the FP32 filter's inner solves (degrees matched to
   // FP32 accuracy; mixed path only, set by block_buffers)
   ChebSetup chB32, chAp32;

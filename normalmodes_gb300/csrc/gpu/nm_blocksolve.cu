@@ -633,21 +633,66 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   // below what the Lanczos recurrence needs to stay free of ghost copies);
   // W itself, the three-term recurrence, the Cholesky and the basis stay
   // FP64.  The FP64 GEMMs are the fallback when the FP32 copy cannot grow.
-  bool orth32 = mixed && c->orth64 == 0;
-  float *W32 = nullptr, *T32 = nullptr, *dH32 = nullptr;
+  bool orth32 = mixed && c->orth != 1;
+  // the projection H = V^T W on the tensor cores (orth 0, where available);
+  // W32 then has a leading dimension that is a multiple of 32 (TMA strides)
+  bool tc = orth32 && c->orth == 0 && gs_tc_available();
+  const size_t ldw32 = ((size_t)n + 31) / 32 * 32;
+  float *W32 = nullptr, *T32 = nullptr, *dH32 = nullptr, *tpart = nullptr;
+  void* d_wmap = nullptr;
   if (orth32) {
-    if (cudaMalloc(&W32, sizeof(float) * L) != cudaSuccess || cudaMalloc(&T32, sizeof(float) * L) != cudaSuccess ||
+    if (cudaMalloc(&W32, sizeof(float) * ldw32 * S) != cudaSuccess ||
+        cudaMalloc(&T32, sizeof(float) * L) != cudaSuccess ||
         cudaMalloc(&dH32, sizeof(float) * (size_t)Kcap * S) != cudaSuccess ||
         ensure32(c, st->V32, n, S) != NM_OK || ensure32(c, st->Z32, n, S) != NM_OK) {
       cudaGetLastError();
-      orth32 = false;
+      orth32 = tc = false;
+    }
+  }
+  if (tc) {
+    std::vector<uint8_t> wm(gs_tc_map_bytes() + 64);
+    void* wmh = (void*)(((uintptr_t)wm.data() + 63) & ~(uintptr_t)63);
+    if (gs_tc_map(W32, n, ldw32, 32, wmh) != NM_OK || cudaMalloc(&d_wmap, gs_tc_map_bytes()) != cudaSuccess ||
+        cudaMalloc(&tpart, sizeof(float) * gs_tc_part_floats(Kcap, n)) != cudaSuccess ||
+        cudaMalloc(&st->d_vmaps, gs_tc_map_bytes() * (size_t)(kMaxCols / Basis::kChunk + 1)) != cudaSuccess) {
+      cudaGetLastError();
+      tc = false;
+    } else {
+      NM_CUDA(c, cudaMemcpyAsync(d_wmap, wmh, gs_tc_map_bytes(), cudaMemcpyHostToDevice, s));
+      NM_CUDA(c, cudaStreamSynchronize(s));
+      st->vmaps.assign(gs_tc_map_bytes() * (size_t)(kMaxCols / Basis::kChunk + 1) + 64, 0);
+      st->vmaps_n = 0;
     }
   }
   auto free32 = [&]() {
     cudaFree(W32);
     cudaFree(T32);
     cudaFree(dH32);
-    W32 = T32 = dH32 = nullptr;
+    cudaFree(tpart);
+    cudaFree(d_wmap);
+    cudaFree(st->d_vmaps);
+    st->d_vmaps = nullptr;
+    st->vmaps_n = 0;
+    W32 = T32 = dH32 = tpart = nullptr;
+    d_wmap = nullptr;
+  };
+  // TMA descriptors for the V32 chunks allocated since the last call
+  auto sync_vmaps = [&]() -> bool {
+    const int nch = (int)st->V32.chunks.size();
+    if (!tc || st->vmaps_n >= nch) return tc;
+    uint8_t* base = (uint8_t*)(((uintptr_t)st->vmaps.data() + 63) & ~(uintptr_t)63);
+    const size_t mb = gs_tc_map_bytes();
+    const int first = st->vmaps_n;
+    for (int q = first; q < nch; ++q)
+      if (gs_tc_map(st->V32.chunks[q], n, st->V32.ld, 64, base + q * mb) != NM_OK) return tc = false;
+    if (cudaMemcpyAsync((uint8_t*)st->d_vmaps + first * mb, base + first * mb, (nch - first) * mb,
+                        cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      cudaGetLastError();
+      return tc = false;
+    }
+    st->vmaps_n = nch;
+    return true;
   };
   // FP32 copy of basis block starting at column K
   auto shadow = [&](int K) {
@@ -847,11 +892,16 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
     // full block Gram-Schmidt, two classical passes: H = V^T W, W -= Z H
     const float onef = 1.0f, zerof = 0.0f;
     for (int pass = 0; orth32 && pass < 2; ++pass) {
-      blk_d2f(Wc, ldw, W32, n, n, S, s);
-      for (int c0 = 0; c0 < K; c0 += Basis::kChunk) {
-        const int w = std::min(Basis::kChunk, K - c0);
-        CB(c, cublasSgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, w, S, n, &onef, st->V32.col(c0), (int)st->V32.ld, W32, n,
-                          &zerof, dH32 + c0, Kcap));
+      blk_d2f(Wc, ldw, W32, ldw32, n, S, s);
+      if (tc && sync_vmaps()) {
+        if ((rc = gs_tc_project(st->d_vmaps, d_wmap, K, n, tpart, dH32, Kcap, c->d_status, s)))
+          return fail(set_err(c, rc, "tensor-core Gram-Schmidt projection"));
+      } else {
+        for (int c0 = 0; c0 < K; c0 += Basis::kChunk) {
+          const int w = std::min(Basis::kChunk, K - c0);
+          CB(c, cublasSgemm(hb, CUBLAS_OP_T, CUBLAS_OP_N, w, S, n, &onef, st->V32.col(c0), (int)st->V32.ld, W32,
+                            (int)ldw32, &zerof, dH32 + c0, Kcap));
+        }
       }
       for (int c0 = 0; c0 < K; c0 += Basis::kChunk) {
         const int w = std::min(Basis::kChunk, K - c0);

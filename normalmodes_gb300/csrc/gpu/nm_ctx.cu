@@ -165,7 +165,7 @@ int nm_create(nm_ctx** out, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, 
   c->precision = o.precision;
   c->verbose = o.verbose;
   c->filter_form = o.filter_form;
-  c->orth64 = o.orth64;
+  c->orth = o.orth;
   c->inner_tol = o.inner_tol;
   c->autotune = o.autotune;
   int rc;

@@ -362,9 +362,15 @@ int gs_tc_splits(int K, int n) {
   return std::min(want, most);
 }
 
-size_t gs_tc_part_floats(int K, int n) {
-  const int kpad = (K + kTcM - 1) / kTcM * kTcM;
-  return (size_t)gs_tc_splits(K, n) * kpad * kTcN;
+// Floats of the partial-sum buffer for every K up to Kmax (the split count
+// falls as K grows, so the product is not monotone in K).
+size_t gs_tc_part_floats(int Kmax, int n) {
+  size_t most = 0;
+  for (int K = 32; K <= std::max(Kmax, 32); K += 32) {
+    const size_t kpad = (size_t)(K + kTcM - 1) / kTcM * kTcM;
+    most = std::max(most, (size_t)gs_tc_splits(K, n) * kpad * kTcN);
+  }
+  return most;
 }
 
 int gs_tc_project(const void* vmaps_dev, const void* wmap_dev, int K, int n, float* part, float* H, int ldh,

@@ -88,7 +88,7 @@ struct nm_ctx {
   int fs = 0, n = 0, np = 0, porder = 1, precision = 0, verbose = 0;
   // mixed block path options (nm_opts): filter form, FP64 Gram-Schmidt,
   // inner B~^-1 accuracy, autotuning
-  int filter_form = 0, orth64 = 0, autotune = 0;
+  int filter_form = 0, orth = 0, autotune = 0;
   double inner_tol = 0.0;
   nmg::Sell<double> A, B, Ap, E, ET;  // scaled, FP64
   nmg::Sell<float> A32, B32, Ap32, E32, ET32;

@@ -42,7 +42,7 @@ class NmCsr(C.Structure):
 class NmOpts(C.Structure):
     _fields_ = [("porder", C.c_int), ("device", C.c_int), ("b_cheb_deg", C.c_int), ("ap_cheb_deg", C.c_int),
                 ("b_bounds", C.c_double * 2), ("ap_bounds", C.c_double * 2), ("precision", C.c_int),
-                ("verbose", C.c_int), ("filter_form", C.c_int), ("orth64", C.c_int), ("inner_tol", C.c_double),
+                ("verbose", C.c_int), ("filter_form", C.c_int), ("orth", C.c_int), ("inner_tol", C.c_double),
                 ("autotune", C.c_int)]
 
 
@@ -256,7 +256,7 @@ class Solver:
 
     def __init__(self, mats: dict, porder: int, device: int = 0, precision: int = NM_PREC_FP64,
                  b_bounds=None, ap_bounds=None, b_cheb_deg: int = 0, ap_cheb_deg: int = 0, verbose: bool = False,
-                 filter_form: int = 0, orth64: int = 0, inner_tol: float = 0.0, autotune: int = 0):
+                 filter_form: int = 0, orth: int = 0, inner_tol: float = 0.0, autotune: int = 0):
         L = lib()
         self.fs = "Ad" in mats
         self._keep = []
@@ -283,7 +283,7 @@ class Solver:
         o.b_cheb_deg = b_cheb_deg
         o.ap_cheb_deg = ap_cheb_deg
         o.filter_form = filter_form
-        o.orth64 = orth64
+        o.orth = orth
         o.inner_tol = inner_tol
         o.autotune = autotune
         if b_bounds is not None:
