@@ -37,6 +37,8 @@ def main(argv=None) -> None:
     ap.add_argument("--refine-maxdeg", type=int, default=0)
     ap.add_argument("--refine-band", type=float, default=0.0)
     ap.add_argument("--skip-fp64", action="store_true", help="mixed path only (no comparison)")
+    ap.add_argument("--orth", type=int, default=0,
+                    help="mixed Gram-Schmidt: 0 tensor-core projection, 1 FP64, 2 cuBLAS SGEMM")
     ap.add_argument("--verbose", action="store_true")
     a = ap.parse_args(argv)
     from normalmodes_gb300.model import Model
@@ -53,7 +55,7 @@ def main(argv=None) -> None:
     runs = [("mixed", NM_PREC_MIXED, 32)] + ([] if (a.fp64_lam or a.skip_fp64) else
                                               [("fp64", NM_PREC_FP64, a.fp64_block)])
     for name, prec, block in runs:
-        with Solver(mats, a.porder, precision=prec, inner_tol=a.inner_tol, verbose=a.verbose) as sv:
+        with Solver(mats, a.porder, precision=prec, inner_tol=a.inner_tol, verbose=a.verbose, orth=a.orth) as sv:
             t = time.perf_counter()
             kw = dict(polish=a.polish, resid_tol=a.resid_tol, refine_sweeps=a.refine_sweeps,
                       refine_maxdeg=a.refine_maxdeg, refine_band=a.refine_band) if name == "mixed" else {}
