@@ -114,7 +114,12 @@ typedef struct {
                          closed by an FP64 Rayleigh-Ritz (0: 2)                 */
   int refine_maxdeg;  /* adaptive refinement: degree cap per block (0: 4000)      */
   double refine_band; /* adaptive refinement: the damped band starts at this
-                         multiple of the block's largest Ritz value (0: 5)     */
+                         multiple of the block's largest Ritz value (0: 8)     */
+  int refine_purge;   /* adaptive refinement, closing (B~^-1 A)/theta step that
+                         removes null-space content: 0 for the blocks whose
+                         lmax / theta is below 2e4 (it multiplies the FP32
+                         rounding of the correction by that ratio), 1 always,
+                         -1 never                                              */
   nm_progress_fn progress; /* host callback at phase boundaries (NULL: none)      */
   void* progress_data;     /* first argument of progress                          */
 } nm_solve_opts;
@@ -310,6 +315,27 @@ int nm_adjoint_gravity(const nm_elem_model* em, int k, const double* X, int ldx,
  *   a degenerate multiplet). */
 int nm_adjoint(nm_ctx* ctx, const nm_elem_model* em, int k, const double* lam, const double* X, int ldx, int mode,
                double tol, double* grad, int* group, int* ngroups);
+
+/* Element-level assembly of the JOB = 1 operators on the GPU (no gravity):
+ * the element matrices of CGE3D_ISO / CGFSE3D_ISO (src/mod_cg_create_matrix.f90:
+ * 103-1266: solid elements, fluid elements, fluid-solid interface faces)
+ * computed per tetrahedron on the device and added into the given CSR
+ * structures (:1269-2033).  em: the mesh, DOF map, nodal material and
+ * reference element (as for nm_adjoint; g0 must be NULL).  Each nm_csr_fill
+ * gives a structure (host rowptr/col, 0-based, sorted columns) and receives
+ * its values (host val, overwritten); solid model: A and B (Ap, E, ET NULL),
+ * fluid-solid model: Ad (as A), B, Ap, E, ET.  seconds (nullable) receives
+ * the device time of the assembly kernel.  NM_ERR_ARG if a structure lacks
+ * an entry an element needs, NM_ERR_NUMERIC for a flat tetrahedron. */
+typedef struct {
+  int nrows;
+  const int* rowptr; /* nrows + 1 */
+  const int* col;    /* rowptr[nrows], ascending within each row */
+  double* val;       /* rowptr[nrows], written */
+} nm_csr_fill;
+int nm_assemble(const nm_elem_model* em, nm_csr_fill* A, nm_csr_fill* B, nm_csr_fill* Ap, nm_csr_fill* E,
+                nm_csr_fill* ET, double* seconds);
+
 
 /* Introspection. */
 typedef struct {

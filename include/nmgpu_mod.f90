@@ -42,6 +42,7 @@ module nmgpu_mod
     real(c_double) :: resid_tol
     integer(c_int) :: refine_sweeps, refine_maxdeg
     real(c_double) :: refine_band
+    integer(c_int) :: refine_purge
     type(c_funptr) :: progress
     type(c_ptr) :: progress_data
   end type nm_solve_opts

@@ -36,6 +36,7 @@ def main(argv=None) -> None:
     ap.add_argument("--refine-sweeps", type=int, default=0)
     ap.add_argument("--refine-maxdeg", type=int, default=0)
     ap.add_argument("--refine-band", type=float, default=0.0)
+    ap.add_argument("--refine-purge", type=int, default=0, help="0 auto, 1 every block, -1 none")
     ap.add_argument("--skip-fp64", action="store_true", help="mixed path only (no comparison)")
     ap.add_argument("--orth", type=int, default=0,
                     help="mixed Gram-Schmidt: 0 tensor-core projection, 1 FP64, 2 cuBLAS SGEMM")
@@ -50,7 +51,7 @@ def main(argv=None) -> None:
     lo, hi = a.interval
     out = {"cells": a.cells, "porder": a.porder, "lateral": a.lateral, "interval_mhz": [lo, hi], "polish": a.polish,
            "gravity": a.gravity, "inner_tol": a.inner_tol, "resid_tol": a.resid_tol,
-           "refine_sweeps": a.refine_sweeps, "refine_maxdeg": a.refine_maxdeg, "refine_band": a.refine_band}
+           "refine_sweeps": a.refine_sweeps, "refine_maxdeg": a.refine_maxdeg, "refine_band": a.refine_band, "refine_purge": a.refine_purge}
     res = {}
     runs = [("mixed", NM_PREC_MIXED, 32)] + ([] if (a.fp64_lam or a.skip_fp64) else
                                               [("fp64", NM_PREC_FP64, a.fp64_block)])
@@ -58,7 +59,8 @@ def main(argv=None) -> None:
         with Solver(mats, a.porder, precision=prec, inner_tol=a.inner_tol, verbose=a.verbose, orth=a.orth) as sv:
             t = time.perf_counter()
             kw = dict(polish=a.polish, resid_tol=a.resid_tol, refine_sweeps=a.refine_sweeps,
-                      refine_maxdeg=a.refine_maxdeg, refine_band=a.refine_band) if name == "mixed" else {}
+                      refine_maxdeg=a.refine_maxdeg, refine_band=a.refine_band,
+                      refine_purge=a.refine_purge) if name == "mixed" else {}
             r = sv.solve(lo, hi, block=block, want_vectors=False, **kw)
             dt = time.perf_counter() - t
         res[name] = r

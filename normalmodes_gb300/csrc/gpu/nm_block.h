@@ -250,8 +250,8 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
 //    space of A, the zero-frequency fluid modes, whose FP32-level content no
 //    polynomial normalised at theta can damp.
 // Any polynomial normalised at theta grows below it: with the band starting
-// at c = band * (largest theta of the block), band = 5, the growth of the
-// lower modes is about D^0.12 for a damping D, and the Rayleigh-Ritz over
+// at c = band * (largest theta of the block), band = 8, the growth of the
+// lower modes is about D^0.06 for a damping D, and the Rayleigh-Ritz over
 // all Ritz vectors that closes each pass removes it along the other wanted
 // modes.  The degree per block of 32 Ritz vectors is the smallest that
 // brings every column's residual below tol_res2 with a margin `safety`,
@@ -259,11 +259,16 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
 //   d = max_j acosh(safety (lmax/theta_j) res2_j / tol_res2)
 //             / acosh(1 + 2 (c - theta_j) / (lmax - c)),
 // clamped to [mindeg, maxdeg]; blocks already below tol_res2 are left alone.
+// The purge multiplies the FP32 rounding of the damping step's correction
+// by up to lmax / theta in the vector and again in the residual, so it runs
+// only on blocks whose lmax / theta_min stays below purge_ratio (purge 0),
+// on every block (1) or on none (-1).
 struct RefineParams {
   double tol_res2 = 1e-7;  // target ||A u - theta B u||_2 / (|theta| ||u||_B)
-  double band = 5.0;
+  double band = 8.0;
   double safety = 4.0;
-  bool purge = true;
+  int purge = 0;
+  double purge_ratio = 2e4;
   int mindeg = 8, maxdeg = 4000;
 };
 struct RefineStats {
@@ -272,7 +277,7 @@ struct RefineStats {
   double max_res2_before = 0.0;  // largest res2 measured before the pass
 };
 int refine_block_degree(const std::vector<double>& theta, const std::vector<double>& res2, double c0, double lmax,
-                        const RefineParams& rp);
+                        const RefineParams& rp, bool purge);
 int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, const RefineParams& rp,
              RefineStats* stats);
 

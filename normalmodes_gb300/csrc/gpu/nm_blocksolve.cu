@@ -1362,13 +1362,13 @@ int kpm_moments_block(nm_ctx* c, double lmin, double lmax, int degree, int nvec,
 }
 
 int refine_block_degree(const std::vector<double>& theta, const std::vector<double>& res2, double c0, double lmax,
-                        const RefineParams& rp) {
+                        const RefineParams& rp, bool purge) {
   double need = 0.0;
   for (size_t j = 0; j < theta.size() && j < res2.size(); ++j) {
     if (!(res2[j] > rp.tol_res2) || !(theta[j] > 0.0)) continue;
     // the closing (B~^-1 A) / theta step multiplies the band's components by
     // up to lmax / theta: the damping has to cover that too
-    const double damp = rp.safety * (rp.purge ? lmax / theta[j] : 1.0) * res2[j] / rp.tol_res2;
+    const double damp = rp.safety * (purge ? lmax / theta[j] : 1.0) * res2[j] / rp.tol_res2;
     const double delta = 2.0 * (c0 - theta[j]) / (lmax - c0);
     if (!(delta > 0.0)) continue;  // at or above the band: not refinable
     need = std::max(need, std::acosh(damp) / std::acosh(1.0 + delta));
@@ -1453,7 +1453,11 @@ int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
     }
     stats.max_res2_before = std::max(stats.max_res2_before, worst);
     const double c0 = std::min(rp.band * thmax, 0.5 * lmax);
-    const int deg = thmax > 0.0 ? refine_block_degree(tb, rb, c0, lmax, rp) : 0;
+    double thmin = thmax;
+    for (double t : tb)
+      if (t > 0.0) thmin = std::min(thmin, t);
+    const bool purge = rp.purge > 0 || (rp.purge == 0 && thmin > 0.0 && lmax / thmin < rp.purge_ratio);
+    const int deg = thmax > 0.0 ? refine_block_degree(tb, rb, c0, lmax, rp, purge) : 0;
     if (deg > 0) {
       const double alpha = 2.0 / (lmax - c0), beta = (lmax + c0) / (lmax - c0);
       FiltEpi ep;  // D_{j+1} = 2 alpha A B~^-1 D_j - 2 beta D_j - D_{j-1} (+ forcing)
@@ -1496,7 +1500,7 @@ int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
       // U += B~^-1 D_deg / T_deg(l(theta))
       blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
       blk_add_colmajor_cols(f.w2, dsc, n, ncol, U + (size_t)j0 * n, n, s);
-      if (rp.purge) {
+      if (purge) {
         // U <- (B~^-1 A / theta) U = U + B~^-1 (A U - theta B U) / theta: exactly
         // zero on the null space of A (the zero-frequency fluid modes, whose
         // FP32-level content the Gram-Schmidt and Ritz products leave in U),

@@ -463,6 +463,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
       rp.tol_res2 = (o.resid_tol > 0 ? o.resid_tol : 1e-10) * std::sqrt((double)n);  // err_ref = res2 / sqrt(N)
       if (o.refine_maxdeg > 0) rp.maxdeg = o.refine_maxdeg;
       if (o.refine_band > 1.0) rp.band = o.refine_band;
+      rp.purge = o.refine_purge;
       const int sweeps = o.refine_sweeps > 0 ? o.refine_sweeps : 2;
       for (int sw = 0; refine && sw < sweeps; ++sw) {
         RefineStats rs;

@@ -51,8 +51,8 @@ class NmSolveOpts(C.Structure):
                 ("mlan_bounds", C.c_int), ("ab_bounds", C.c_double * 2), ("damping", C.c_int),
                 ("want_vectors", C.c_int), ("unscale", C.c_int), ("use_graph", C.c_int), ("block", C.c_int),
                 ("polish", C.c_int), ("resid_tol", C.c_double), ("refine_sweeps", C.c_int),
-                ("refine_maxdeg", C.c_int), ("refine_band", C.c_double), ("progress", C.c_void_p),
-                ("progress_data", C.c_void_p)]
+                ("refine_maxdeg", C.c_int), ("refine_band", C.c_double), ("refine_purge", C.c_int),
+                ("progress", C.c_void_p), ("progress_data", C.c_void_p)]
 
 
 # void (*)(void* data, int phase, int done, int total)
@@ -111,6 +111,32 @@ def _elem_model(mesh: dict, ref: dict, fluid_solid: bool, g0=None):
     return em, keep
 
 
+def assemble(model) -> tuple:
+    """nm_assemble: the JOB = 1 operators of `model` (normalmodes_gb300.model.Model)
+    assembled element by element on the GPU into the model's own CSR
+    structures.  Returns ({name: values}, kernel seconds)."""
+    mats = model.operators()
+    fs = "Ad" in mats
+    em, keep = _elem_model(model.mesh(), model.reference(), fs)
+    names = ["Ad", "B", "Ap", "E", "ET"] if fs else ["A", "B"]
+    vals, fills = {}, {}
+    for nm in names:
+        m = mats[nm]
+        rp = np.ascontiguousarray(m.rowptr, dtype=np.int32)
+        ci = np.ascontiguousarray(m.col, dtype=np.int32)
+        vals[nm] = np.zeros(len(ci))
+        keep[nm + "_rp"], keep[nm + "_ci"] = rp, ci
+        fills[nm] = NmCsrFill(m.shape[0], rp.ctypes.data_as(C.POINTER(C.c_int)), ci.ctypes.data_as(C.POINTER(C.c_int)),
+                              _dp(vals[nm]))
+    ref = lambda k: C.byref(fills[k]) if k in fills else None
+    sec = C.c_double()
+    rc = lib().nm_assemble(C.byref(em), ref("Ad" if fs else "A"), ref("B"), ref("Ap"), ref("E"), ref("ET"),
+                           C.byref(sec))
+    if rc != 0:
+        raise NmError(rc, "nm_assemble failed")
+    return vals, sec.value
+
+
 def adjoint_gravity(mesh: dict, ref: dict, g0, X, P=None, fluid_solid: bool = False) -> np.ndarray:
     """nm_adjoint_gravity (host code, no GPU): the reference-gravity terms of
     the per-pair sensitivities, (k, ntet, 3)."""
@@ -128,6 +154,11 @@ def adjoint_gravity(mesh: dict, ref: dict, g0, X, P=None, fluid_solid: bool = Fa
     if rc != 0:
         raise NmError(rc, "nm_adjoint_gravity failed")
     return grad
+
+
+class NmCsrFill(C.Structure):
+    _fields_ = [("nrows", C.c_int), ("rowptr", C.POINTER(C.c_int)), ("col", C.POINTER(C.c_int)),
+                ("val", C.POINTER(C.c_double))]
 
 
 class NmSlice(C.Structure):
@@ -215,6 +246,7 @@ def lib() -> C.CDLL:
                                      C.c_ulonglong, dp]
         L.nm_kpm_moments_ctx.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_ulonglong, dp]
         L.nm_test_gather_shape.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.nm_assemble.argtypes = [C.POINTER(NmElemModel)] + [C.POINTER(NmCsrFill)] * 5 + [dp]
         L.nm_test_gs_tc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int]
         L.nm_kpm_count.argtypes = [dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, dp]
         L.nm_kpm_slices.argtypes = [dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
@@ -347,13 +379,14 @@ class Solver:
     @staticmethod
     def _solve_opts(maxit=0, tol=0.0, ab_bounds=None, want_vectors=True, unscale=False, use_graph=True, damping=1,
                     mlan_bounds=0, block=0, polish=0, resid_tol=0.0, refine_sweeps=0, refine_maxdeg=0,
-                    progress=None, refine_band=0.0) -> "NmSolveOpts":
+                    progress=None, refine_band=0.0, refine_purge=0) -> "NmSolveOpts":
         o = NmSolveOpts()
         lib().nm_default_solve_opts(C.byref(o))
         o.resid_tol = resid_tol
         o.refine_sweeps = refine_sweeps
         o.refine_maxdeg = refine_maxdeg
         o.refine_band = refine_band
+        o.refine_purge = refine_purge
         if progress is not None:  # an NM_PROGRESS_FN the caller keeps alive for the call
             o.progress = C.cast(progress, C.c_void_p)
         o.maxit = maxit
@@ -390,7 +423,7 @@ class Solver:
               want_vectors: bool = True, unscale: bool = False, use_graph: bool = True, damping: int = 1,
               mlan_bounds: int = 0, allow_noconv: bool = False, block: int = 0, polish: int = 0,
               resid_tol: float = 0.0, refine_sweeps: int = 0, refine_maxdeg: int = 0,
-              progress=None, refine_band: float = 0.0) -> SolveResult:
+              progress=None, refine_band: float = 0.0, refine_purge: int = 0) -> SolveResult:
         """nm_solve on [lowfreq, upfreq] mHz.  `progress`, if given, is a
         Python callable progress(phase, done, total) called at the solve's
         phase and block boundaries (NM_PHASE_*), stream drained."""
@@ -399,7 +432,7 @@ class Solver:
         if progress is not None:
             cb = NM_PROGRESS_FN(lambda _d, ph, done, tot: progress(ph, done, tot))
         o = self._solve_opts(maxit, tol, ab_bounds, want_vectors, unscale, use_graph, damping, mlan_bounds, block,
-                             polish, resid_tol, refine_sweeps, refine_maxdeg, cb, refine_band)
+                             polish, resid_tol, refine_sweeps, refine_maxdeg, cb, refine_band, refine_purge)
         r = NmResult()
         rc = L.nm_solve(self._h, lowfreq, upfreq, C.byref(o), C.byref(r))
         try:

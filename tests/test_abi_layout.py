@@ -18,7 +18,7 @@ INC = os.path.join(ROOT, "include")
 
 STRUCTS = {
     "nm_csr": G.NmCsr, "nm_opts": G.NmOpts, "nm_solve_opts": G.NmSolveOpts, "nm_result": G.NmResult,
-    "nm_elem_model": G.NmElemModel, "nm_slice": G.NmSlice, "nm_kpm_opts": G.NmKpmOpts, "nm_info": G.NmInfo,
+    "nm_elem_model": G.NmElemModel, "nm_slice": G.NmSlice, "nm_csr_fill": G.NmCsrFill, "nm_kpm_opts": G.NmKpmOpts, "nm_info": G.NmInfo,
     "nmm_ball_opts": M.BallOpts, "nmm_info_t": M.Info,
 }
 
