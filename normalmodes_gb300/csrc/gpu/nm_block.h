@@ -269,6 +269,7 @@ struct RefineParams {
   double safety = 4.0;
   int purge = 0;
   double purge_ratio = 2e4;
+  int purge_damp = 2;  // damping passes before a purge
   int mindeg = 8, maxdeg = 4000;
 };
 struct RefineStats {

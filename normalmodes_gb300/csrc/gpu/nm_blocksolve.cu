@@ -1428,37 +1428,47 @@ int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
     const int j0 = b * S, ncol = std::min(S, nc - j0);
     for (int col = 0; col < S; ++col) th[col] = col < ncol ? theta[j0 + col] : 0.0;
     NM_CUDA(c, cudaMemcpyAsync(dth, th.data(), sizeof(double) * S, cudaMemcpyHostToDevice, s));
-    // FP64 residual R = A U - theta B U (reference operators and degrees);
-    // the last block's padding columns are zero
-    blk_from_colmajor_cols(U + (size_t)j0 * n, n, n, ncol, sin_, s);
-    if (c->fs) {
-      blk_et<double, double>(st->ET64, sin_, x0, s, st->gA64);
-      blk_ap_solve<double, double>(c, st->Ap64, x0, y0, apw);
-    }
-    blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sAU, nullptr, nullptr, nullptr,
-                            ep0, s, st->gA64);
-    blk_mass_spmv<double>(st->M64, sin_, sBU, s);
-    blk_colres(sAU, sBU, sin_, dth, n, dred, s);
-    NM_CUDA(c, cudaMemcpyAsync(sums.data(), dsums, sizeof(double) * 2 * S, cudaMemcpyDeviceToHost, s));
-    NM_CUDA(c, cudaStreamSynchronize(s));
-    std::vector<double> tb, rb;
-    double thmax = 0.0, worst = 0.0;
+    // FP64 residual R = A U - theta B U of the block (reference operators and
+    // degrees) into sAU / sBU, and every column's res2; padding columns are zero
+    auto residual = [&](std::vector<double>& rb) -> int {
+      blk_from_colmajor_cols(U + (size_t)j0 * n, n, n, ncol, sin_, s);
+      if (c->fs) {
+        blk_et<double, double>(st->ET64, sin_, x0, s, st->gA64);
+        blk_ap_solve<double, double>(c, st->Ap64, x0, y0, apw);
+      }
+      blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sAU, nullptr, nullptr, nullptr,
+                              ep0, s, st->gA64);
+      blk_mass_spmv<double>(st->M64, sin_, sBU, s);
+      blk_colres(sAU, sBU, sin_, dth, n, dred, s);
+      NM_CUDA(c, cudaMemcpyAsync(sums.data(), dsums, sizeof(double) * 2 * S, cudaMemcpyDeviceToHost, s));
+      NM_CUDA(c, cudaStreamSynchronize(s));
+      rb.assign(ncol, 0.0);
+      for (int col = 0; col < ncol; ++col) {
+        const double ub = sums[S + col];
+        rb[col] = ub > 0.0 && th[col] != 0.0 ? std::sqrt(sums[col] / ub) / std::fabs(th[col]) : 0.0;
+      }
+      return NM_OK;
+    };
+    std::vector<double> tb(th.begin(), th.begin() + ncol), rb;
+    if ((rc = residual(rb))) return rc;
+    double thmax = 0.0, thmin = 0.0, worst = 0.0;
     for (int col = 0; col < ncol; ++col) {
-      const double ub = sums[S + col];
-      const double r2 = ub > 0.0 && th[col] != 0.0 ? std::sqrt(sums[col] / ub) / std::fabs(th[col]) : 0.0;
-      tb.push_back(th[col]);
-      rb.push_back(r2);
       thmax = std::max(thmax, th[col]);
-      worst = std::max(worst, r2);
+      if (th[col] > 0.0) thmin = thmin > 0.0 ? std::min(thmin, th[col]) : th[col];
+      worst = std::max(worst, rb[col]);
     }
     stats.max_res2_before = std::max(stats.max_res2_before, worst);
     const double c0 = std::min(rp.band * thmax, 0.5 * lmax);
-    double thmin = thmax;
-    for (double t : tb)
-      if (t > 0.0) thmin = std::min(thmin, t);
     const bool purge = rp.purge > 0 || (rp.purge == 0 && thmin > 0.0 && lmax / thmin < rp.purge_ratio);
-    const int deg = thmax > 0.0 ? refine_block_degree(tb, rb, c0, lmax, rp, purge) : 0;
-    if (deg > 0) {
+    // damping passes: one, or purge_damp before a purge (each pass damps the
+    // FP32 rounding the previous one left, which the purge would multiply)
+    const int npass = purge ? std::max(1, rp.purge_damp) : 1;
+    bool damped = false;
+    for (int pass = 0; pass < npass; ++pass) {
+      if (pass > 0 && (rc = residual(rb))) return rc;
+      const int deg = thmax > 0.0 ? refine_block_degree(tb, rb, c0, lmax, rp, purge) : 0;
+      if (deg <= 0) break;
+      damped = true;
       const double alpha = 2.0 / (lmax - c0), beta = (lmax + c0) / (lmax - c0);
       FiltEpi ep;  // D_{j+1} = 2 alpha A B~^-1 D_j - 2 beta D_j - D_{j-1} (+ forcing)
       ep.mode = 1;
@@ -1490,7 +1500,8 @@ int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
           blk_et<float, float>(st->ET32, f.w2, f.x0, s, st->gA32);
           blk_ap_solve<float, float>(c, st->Ap32, f.x0, f.y0, f.apwork);
         }
-        blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s, st->gA32);
+        blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s,
+                              st->gA32);
         blk_force(vkp1, f.zin, dfor + (size_t)j * S, L, s);
         float* t = vkm1;
         vkm1 = vk;
@@ -1500,31 +1511,24 @@ int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
       // U += B~^-1 D_deg / T_deg(l(theta))
       blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
       blk_add_colmajor_cols(f.w2, dsc, n, ncol, U + (size_t)j0 * n, n, s);
-      if (purge) {
-        // U <- (B~^-1 A / theta) U = U + B~^-1 (A U - theta B U) / theta: exactly
-        // zero on the null space of A (the zero-frequency fluid modes, whose
-        // FP32-level content the Gram-Schmidt and Ritz products leave in U),
-        // up to the accuracy of B~^-1 B; the residual is FP64 and small, so the
-        // FP32 solve adds rounding far below FP64 level relative to U
-        blk_from_colmajor_cols(U + (size_t)j0 * n, n, n, ncol, sin_, s);
-        if (c->fs) {
-          blk_et<double, double>(st->ET64, sin_, x0, s, st->gA64);
-          blk_ap_solve<double, double>(c, st->Ap64, x0, y0, apw);
-        }
-        blk_amv<double, double>(st->A64, c->fs ? &st->E64 : nullptr, sin_, y0, sAU, nullptr, nullptr, nullptr, ep0, s,
-                                st->gA64);
-        blk_mass_spmv<double>(st->M64, sin_, sBU, s);
-        blk_resid_f32(sAU, sBU, dth, f.zin, 1.0f, L, s);
-        blk_mass_solve<float, float>(c, st->M32, f.zin, f.w2, f.bwork);
-        for (int col = 0; col < S; ++col) sc[col] = col < ncol && th[col] > 0.0 ? 1.0 / th[col] : 0.0;
-        NM_CUDA(c, cudaMemcpyAsync(dsc, sc.data(), sizeof(double) * S, cudaMemcpyHostToDevice, s));
-        blk_add_colmajor_cols(f.w2, dsc, n, ncol, U + (size_t)j0 * n, n, s);
-        ++c->n_amv;
-      }
       c->n_amv += (long long)deg * S;
-      stats.blocks += 1;
       stats.steps += deg;
       stats.max_deg = std::max(stats.max_deg, deg);
+    }
+    if (damped) stats.blocks += 1;
+    if (damped && purge) {
+      // U <- (B~^-1 A / theta) U = U + B~^-1 (A U - theta B U) / theta: exactly
+      // zero on the null space of A (the zero-frequency fluid modes, whose
+      // FP32-level content the Gram-Schmidt and Ritz products leave in U),
+      // up to the accuracy of B~^-1 B; the residual is FP64 and small, so the
+      // FP32 solve adds rounding far below FP64 level relative to U
+      if ((rc = residual(rb))) return rc;
+      blk_resid_f32(sAU, sBU, dth, f.zin, 1.0f, L, s);
+      blk_mass_solve<float, float>(c, st->M32, f.zin, f.w2, f.bwork);
+      for (int col = 0; col < S; ++col) sc[col] = col < ncol && th[col] > 0.0 ? 1.0 / th[col] : 0.0;
+      NM_CUDA(c, cudaMemcpyAsync(dsc, sc.data(), sizeof(double) * S, cudaMemcpyHostToDevice, s));
+      blk_add_colmajor_cols(f.w2, dsc, n, ncol, U + (size_t)j0 * n, n, s);
+      ++c->n_amv;
     }
     NM_CUDA(c, cudaGetLastError());
     progress(c, NM_PHASE_REFINE, b + 1, nblk);
