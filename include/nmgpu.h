@@ -115,11 +115,10 @@ typedef struct {
   int refine_maxdeg;  /* adaptive refinement: degree cap per block (0: 4000)      */
   double refine_band; /* adaptive refinement: the damped band starts at this
                          multiple of the block's largest Ritz value (0: 8)     */
-  int refine_purge;   /* adaptive refinement, closing (B~^-1 A)/theta step that
-                         removes null-space content: 0 for the blocks whose
-                         lmax / theta is below 2e4 (it multiplies the FP32
-                         rounding of the correction by that ratio), 1 always,
-                         -1 never                                              */
+  int refine_purge;   /* adaptive refinement polynomial: 0 or 1 with the factor
+                         x / theta, which removes the Ritz vectors' content in
+                         the null space of A (the zero-frequency fluid modes);
+                         -1 without it                                          */
   nm_progress_fn progress; /* host callback at phase boundaries (NULL: none)      */
   void* progress_data;     /* first argument of progress                          */
 } nm_solve_opts;

@@ -246,9 +246,9 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
 //  * T_d(l(.)) / T_d(l(theta)) damps the band [c, lmax], where FP32 rounding
 //    of the filter left components of relative size ~1e-7 that the residual
 //    weighs by lambda / theta (up to 1e6 for the lowest modes);
-//  * x / theta (one step U + B~^-1 R / theta, "purge") is zero on the null
-//    space of A, the zero-frequency fluid modes, whose FP32-level content no
-//    polynomial normalised at theta can damp.
+//  * x / theta is zero on the null space of A, the zero-frequency fluid
+//    modes, whose FP32-level content (from the FP32 Ritz and Gram-Schmidt
+//    products) no polynomial normalised at theta can damp.
 // Any polynomial normalised at theta grows below it: with the band starting
 // at c = band * (largest theta of the block), band = 8, the growth of the
 // lower modes is about D^0.06 for a damping D, and the Rayleigh-Ritz over
@@ -259,17 +259,14 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
 //   d = max_j acosh(safety (lmax/theta_j) res2_j / tol_res2)
 //             / acosh(1 + 2 (c - theta_j) / (lmax - c)),
 // clamped to [mindeg, maxdeg]; blocks already below tol_res2 are left alone.
-// The purge multiplies the FP32 rounding of the damping step's correction
-// by up to lmax / theta in the vector and again in the residual, so it runs
-// only on blocks whose lmax / theta_min stays below purge_ratio (purge 0),
-// on every block (1) or on none (-1).
+// purge >= 0: h with the factor x / theta, applied as one three-term
+// recurrence for (x T_d(l(x)) - theta T_d(l(theta))) / (x - theta), so no
+// two large FP32 terms cancel; purge < 0: h = T_d(l(x)) / T_d(l(theta)).
 struct RefineParams {
   double tol_res2 = 1e-7;  // target ||A u - theta B u||_2 / (|theta| ||u||_B)
   double band = 8.0;
   double safety = 4.0;
   int purge = 0;
-  double purge_ratio = 2e4;
-  int purge_damp = 2;  // damping passes before a purge
   int mindeg = 8, maxdeg = 4000;
 };
 struct RefineStats {

@@ -1459,76 +1459,89 @@ int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
     }
     stats.max_res2_before = std::max(stats.max_res2_before, worst);
     const double c0 = std::min(rp.band * thmax, 0.5 * lmax);
-    const bool purge = rp.purge > 0 || (rp.purge == 0 && thmin > 0.0 && lmax / thmin < rp.purge_ratio);
-    // damping passes: one, or purge_damp before a purge (each pass damps the
-    // FP32 rounding the previous one left, which the purge would multiply)
-    const int npass = purge ? std::max(1, rp.purge_damp) : 1;
-    bool damped = false;
-    for (int pass = 0; pass < npass; ++pass) {
-      if (pass > 0 && (rc = residual(rb))) return rc;
-      const int deg = thmax > 0.0 ? refine_block_degree(tb, rb, c0, lmax, rp, purge) : 0;
-      if (deg <= 0) break;
-      damped = true;
+    const bool purge = rp.purge >= 0 && thmin > 0.0;
+    // One pass of U <- h(B~^-1 A) U in correction form, driven by the FP64
+    // residual R (in sAU / sBU), all vectors FP32:
+    //  * damping only (no purge), h = T_d(l(x)) / T_d(l(theta)):
+    //      D_0 = 0, D_1 = alpha R, D_{j+1} = 2 l(A B~^-1) D_j - D_{j-1} + 2 alpha s_j R,
+    //      U += B~^-1 D_d / s_d;
+    //  * with the null-space factor, h = (x / theta) T_d(l(x)) / T_d(l(theta)),
+    //    written as (x s_d(x) - theta s_d(theta)) = (x - theta) Q_d(x) with
+    //      Q_0 = 1, Q_1 = alpha (x + theta) - beta,
+    //      Q_{j+1} = 2 l(x) Q_j - Q_{j-1} + 2 alpha theta s_j,
+    //    i.e. E_0 = R, E_1 = alpha A B~^-1 R + (alpha theta - beta) R,
+    //      E_{j+1} = 2 l(A B~^-1) E_j - E_{j-1} + 2 alpha theta s_j R,
+    //      U += B~^-1 E_d / (theta s_d);
+    // s_j = T_j(l(theta)) per column, l(x) = alpha x - beta.  Every E_j stays
+    // of the size of the components it corrects (no two large terms cancel),
+    // so the FP32 rounding stays relative to the correction, and Q_d(0) =
+    // s_d makes the correction remove U's null-space content exactly.
+    const int deg = thmax > 0.0 ? refine_block_degree(tb, rb, c0, lmax, rp, purge) : 0;
+    if (deg > 0) {
       const double alpha = 2.0 / (lmax - c0), beta = (lmax + c0) / (lmax - c0);
-      FiltEpi ep;  // D_{j+1} = 2 alpha A B~^-1 D_j - 2 beta D_j - D_{j-1} (+ forcing)
+      FiltEpi ep;  // out = 2 alpha A B~^-1 v - 2 beta v - vkm1
       ep.mode = 1;
       ep.s = 2.0 * alpha;
       ep.cc = beta / alpha;
       ep.pm = 1.0;
       ep.mu = 0.0;
+      std::vector<float> f1(S, 0.0f);
       for (int col = 0; col < S; ++col) {
-        const double l = alpha * th[col] - beta;
-        const bool skip = col >= ncol || !(l < -1.0 - 1e-12);
+        const double t = th[col], l = alpha * t - beta;
+        const bool skip = col >= ncol || !(l < -1.0 - 1e-12) || !(t > 0.0);
+        const double w = purge ? t : 1.0;  // forcing weight theta for the Q recurrence
         double tm1 = 1.0, tj = l;
         for (int j = 1; j < deg; ++j) {
-          forc[(size_t)j * S + col] = skip ? 0.0f : (float)(2.0 * alpha * tj);
+          forc[(size_t)j * S + col] = skip ? 0.0f : (float)(2.0 * alpha * w * tj);
           const double tn = 2.0 * l * tj - tm1;
           tm1 = tj;
           tj = tn;
         }
-        sc[col] = skip || !std::isfinite(tj) ? 0.0 : 1.0 / tj;  // 1 / T_deg(l(theta))
+        sc[col] = skip || !std::isfinite(tj) ? 0.0 : 1.0 / (w * tj);  // 1 / (theta s_d) or 1 / s_d
+        f1[col] = skip ? 0.0f : (float)(alpha * t);                  // E_1 term alpha theta R
       }
       NM_CUDA(c, cudaMemcpyAsync(dsc, sc.data(), sizeof(double) * S, cudaMemcpyHostToDevice, s));
       NM_CUDA(c, cudaMemcpyAsync(dfor, forc.data(), sizeof(float) * (size_t)S * deg, cudaMemcpyHostToDevice, s));
-      blk_resid_f32(sAU, sBU, dth, f.zin, 1.0f, L, s);
-      blk_resid_f32(sAU, sBU, dth, f.vk, (float)alpha, L, s);
-      NM_CUDA(c, cudaMemsetAsync(f.vkm1, 0, sizeof(float) * L, s));
       float *vk = f.vk, *vkm1 = f.vkm1, *vkp1 = f.vkp1;
-      for (int j = 1; j < deg; ++j) {
-        blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
+      blk_resid_f32(sAU, sBU, dth, f.zin, 1.0f, L, s);  // R in FP32
+      auto a_op = [&](const float* in, float* out, const FiltEpi& e, const float* km1) {
+        blk_mass_solve<float, float>(c, st->M32, in, f.w2, f.bwork);
         if (c->fs) {
           blk_et<float, float>(st->ET32, f.w2, f.x0, s, st->gA32);
           blk_ap_solve<float, float>(c, st->Ap32, f.x0, f.y0, f.apwork);
         }
-        blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, vkp1, vk, vkm1, f.yout, ep, s,
+        blk_amv<float, float>(st->A32, c->fs ? &st->E32 : nullptr, f.w2, f.y0, out, in, km1, f.yout, e, s,
                               st->gA32);
+      };
+      if (purge) {
+        // E_0 = R (vkm1), E_1 = alpha A B~^-1 R - beta R + alpha theta R (vk)
+        NM_CUDA(c, cudaMemcpyAsync(vkm1, f.zin, sizeof(float) * L, cudaMemcpyDeviceToDevice, s));
+        FiltEpi e1 = ep;
+        e1.s = alpha;
+        e1.pm = 0.0;
+        a_op(f.zin, vk, e1, vkm1);
+        NM_CUDA(c, cudaMemcpyAsync(dfor, f1.data(), sizeof(float) * S, cudaMemcpyHostToDevice, s));
+        blk_force(vk, f.zin, dfor, L, s);  // slot 0 of the forcing table holds alpha theta
+      } else {
+        // D_0 = 0, D_1 = alpha R
+        blk_resid_f32(sAU, sBU, dth, vk, (float)alpha, L, s);
+        NM_CUDA(c, cudaMemsetAsync(vkm1, 0, sizeof(float) * L, s));
+      }
+      for (int j = 1; j < deg; ++j) {
+        a_op(vk, vkp1, ep, vkm1);
         blk_force(vkp1, f.zin, dfor + (size_t)j * S, L, s);
         float* t = vkm1;
         vkm1 = vk;
         vk = vkp1;
         vkp1 = t;
       }
-      // U += B~^-1 D_deg / T_deg(l(theta))
+      // U += B~^-1 (E_d or D_d) * sc_col
       blk_mass_solve<float, float>(c, st->M32, vk, f.w2, f.bwork);
       blk_add_colmajor_cols(f.w2, dsc, n, ncol, U + (size_t)j0 * n, n, s);
-      c->n_amv += (long long)deg * S;
+      c->n_amv += (long long)(deg + (purge ? 1 : 0)) * S;
       stats.steps += deg;
       stats.max_deg = std::max(stats.max_deg, deg);
-    }
-    if (damped) stats.blocks += 1;
-    if (damped && purge) {
-      // U <- (B~^-1 A / theta) U = U + B~^-1 (A U - theta B U) / theta: exactly
-      // zero on the null space of A (the zero-frequency fluid modes, whose
-      // FP32-level content the Gram-Schmidt and Ritz products leave in U),
-      // up to the accuracy of B~^-1 B; the residual is FP64 and small, so the
-      // FP32 solve adds rounding far below FP64 level relative to U
-      if ((rc = residual(rb))) return rc;
-      blk_resid_f32(sAU, sBU, dth, f.zin, 1.0f, L, s);
-      blk_mass_solve<float, float>(c, st->M32, f.zin, f.w2, f.bwork);
-      for (int col = 0; col < S; ++col) sc[col] = col < ncol && th[col] > 0.0 ? 1.0 / th[col] : 0.0;
-      NM_CUDA(c, cudaMemcpyAsync(dsc, sc.data(), sizeof(double) * S, cudaMemcpyHostToDevice, s));
-      blk_add_colmajor_cols(f.w2, dsc, n, ncol, U + (size_t)j0 * n, n, s);
-      ++c->n_amv;
+      stats.blocks += 1;
     }
     NM_CUDA(c, cudaGetLastError());
     progress(c, NM_PHASE_REFINE, b + 1, nblk);
