@@ -234,12 +234,14 @@ __device__ __forceinline__ XT ld(const XT* p) {
 // between them and can be in flight together.  CTAs take consecutive rows;
 // rows are numbered along a space-filling curve, so the rows in flight at
 // any time form a compact piece of the mesh whose neighbour rows stay in L2.
-template <typename VT, typename XT, int NC, int MODE, int MAXT>
+template <typename VT, typename XT, int NC, int MODE, int MAXT, int UNR = 4>
 __global__ void __launch_bounds__(MAXT, 1)
     k_mass_cheb(int ng, const int* __restrict__ rp, const int* __restrict__ ci, const VT* __restrict__ mv,
                 const XT* __restrict__ b, const XT* __restrict__ xcur, const XT* xprev, XT* xout, XT a, XT c,
                 XT inv_theta, int sweep) {
-  constexpr int UNR = 4;  // gathers in flight per warp
+  // UNR gathers in flight per warp; a batch's last group is padded with
+  // zero-weight entries on the warp's own row (exact: adds +0), so no
+  // neighbour is gathered alone
   const int lane = threadIdx.x & (kBlk - 1);
   const RowRange rr = row_range(ng, sweep);
   for (int g = rr.r; g < rr.end; g += rr.step) {
@@ -261,14 +263,17 @@ __global__ void __launch_bounds__(MAXT, 1)
     const int cnt = min(kBlk, e1 - base);
     const int myh = lane < cnt ? __ldg(ci + base + lane) : 0;
     const XT mym = lane < cnt ? (XT)__ldg(mv + base + lane) : (XT)0;
-    int k = 0;
-    for (; k + UNR <= cnt; k += UNR) {
+    for (int k = 0; k < cnt; k += UNR) {
       const XT* xs[UNR];
       XT m[UNR];
 #pragma unroll
       for (int u = 0; u < UNR; ++u) {
-        xs[u] = src + (size_t)NC * __shfl_sync(0xffffffffu, myh, k + u) * kBlk + lane;
-        m[u] = __shfl_sync(0xffffffffu, mym, k + u);
+        const int q = (k + u) & 31;
+        const int h = __shfl_sync(0xffffffffu, myh, q);
+        const XT mq = __shfl_sync(0xffffffffu, mym, q);
+        const bool in = k + u < cnt;
+        xs[u] = src + (size_t)NC * (in ? h : g) * kBlk + lane;
+        m[u] = in ? mq : (XT)0;
       }
       XT v[UNR][NC];
 #pragma unroll
@@ -279,12 +284,6 @@ __global__ void __launch_bounds__(MAXT, 1)
       for (int u = 0; u < UNR; ++u)
 #pragma unroll
         for (int p = 0; p < NC; ++p) t[p] = fm<XT>(m[u], v[u][p], t[p]);
-    }
-    for (; k < cnt; ++k) {
-      const XT* xs = src + (size_t)NC * __shfl_sync(0xffffffffu, myh, k) * kBlk + lane;
-      const XT m = __shfl_sync(0xffffffffu, mym, k);
-#pragma unroll
-      for (int p = 0; p < NC; ++p) t[p] = fm<XT>(m, __ldg(xs + p * kBlk), t[p]);
     }
   }
 #pragma unroll
@@ -795,13 +794,18 @@ void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT*
   const size_t len = (size_t)NC * ng * kBlk;
   XT* buf[2] = {work, work + len};  // x_j lives in buf[j & 1]
   const XT it = (XT)ch.inv_theta;
-  const bool vec = cfg.vec < 0 ? gather_vec(NC) : cfg.vec != 0;
-  const int thr = launch_threads(cfg);
-  const int sw = cfg.sweep;
+  // kernel: 0 one value per lane, 4 gathers in flight; 1 16-byte vector
+  // gathers (k_gcheb); 2 one value per lane, 8 gathers in flight (CTAs of
+  // at most 256 threads)
+  const int kind = cfg.vec < 0 ? (gather_vec(NC) ? 1 : 0) : cfg.vec;
+  const bool vec = kind == 1, deep = kind == 2;
+  const int thr = deep ? std::min(kT, launch_threads(cfg)) : launch_threads(cfg);
+  const int sw = deep ? 0 : cfg.sweep;
   const bool big = thr > kT;  // CTAs above 256 threads use the kernels compiled for 1024
-  const void* fn = vec ? (big ? (const void*)k_gcheb<VT, XT, NC, 2, kTMax> : (const void*)k_gcheb<VT, XT, NC, 2, kT>)
-                       : (big ? (const void*)k_mass_cheb<VT, XT, NC, 2, kTMax>
-                              : (const void*)k_mass_cheb<VT, XT, NC, 2, kT>);
+  const void* fn = deep ? (const void*)k_mass_cheb<VT, XT, NC, 2, kT, 8>
+                   : vec ? (big ? (const void*)k_gcheb<VT, XT, NC, 2, kTMax> : (const void*)k_gcheb<VT, XT, NC, 2, kT>)
+                         : (big ? (const void*)k_mass_cheb<VT, XT, NC, 2, kTMax>
+                                : (const void*)k_mass_cheb<VT, XT, NC, 2, kT>);
   const int grid = row_grid(fn, thr, ng, sw);
   for (int j = 1; j <= ch.deg; ++j) {
     const XT a = (XT)ch.a[j - 1], c = (XT)ch.c[j - 1];
@@ -823,7 +827,13 @@ void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT*
     else                                                                                                      \
       k_mass_cheb<VT, XT, NC, MODE, kT><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it, sw); \
   } while (0)
-    if (vec) {
+#define NM_MD(MODE) \
+  k_mass_cheb<VT, XT, NC, MODE, kT, 8><<<grid, thr, 0, s>>>(ng, M.rp, M.ci, M.v, b, cur, prev, out, a, c, it, 0)
+    if (deep) {
+      if (j == 1) NM_MD(0);
+      else if (j == 2) NM_MD(1);
+      else NM_MD(2);
+    } else if (vec) {
       if (j == 1) NM_MV(0);
       else if (j == 2) NM_MV(1);
       else NM_MV(2);
@@ -834,6 +844,7 @@ void gather_cheb(const GCsr<VT>& M, const ChebSetup& ch, const XT* b, XT* x, XT*
     }
 #undef NM_MC
 #undef NM_MV
+#undef NM_MD
     nmg::add_launches(1);
   }
 }
@@ -865,6 +876,11 @@ void prefer_l1_set() {
                       (const void*)k_amv3<VT, XT, false, 0, MAXT>,  (const void*)k_amv3<VT, XT, false, 1, MAXT>,
                       (const void*)k_et<VT, XT, MAXT>};
   for (const void* f : fs) cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  if (MAXT == kT)
+    for (const void* f : {(const void*)k_mass_cheb<VT, XT, 3, 0, kT, 8>, (const void*)k_mass_cheb<VT, XT, 3, 1, kT, 8>,
+                          (const void*)k_mass_cheb<VT, XT, 3, 2, kT, 8>, (const void*)k_mass_cheb<VT, XT, 1, 0, kT, 8>,
+                          (const void*)k_mass_cheb<VT, XT, 1, 1, kT, 8>, (const void*)k_mass_cheb<VT, XT, 1, 2, kT, 8>})
+      cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
 }
 
 void blk_prefer_l1() {

@@ -51,9 +51,10 @@ template <typename T>
 void free_g(GCsr<T>& g);
 
 // Launch shape of the gather Chebyshev kernels: vec 1 = 16-byte vector
-// gathers (k_gcheb), 0 = one value per lane (k_mass_cheb), -1 = the default
-// for the component count; threads per CTA (one row per warp).  Picked per
-// context by the autotuner (block_autotune).
+// gathers (k_gcheb), 0 = one value per lane (k_mass_cheb, 4 gathers in
+// flight per warp), 2 = the same with 8 in flight, -1 = the default for the
+// component count; threads per CTA (one row per warp).  Picked per context
+// by the autotuner (block_autotune).
 struct GatherCfg {
   int vec = -1;
   int threads = 256;

@@ -318,13 +318,13 @@ int block_autotune(nm_ctx* c) {
   NM_CUDA(c, cudaEventCreate(&e1));
   // gather shape x CTA size x row schedule (plain: 8 or 4 rows per CTA;
   // sweep: one contiguous row range per CTA)
-  const GatherCfg cands[8] = {{0, 256, 0},  {1, 256, 0},  {0, 128, 0}, {1, 128, 0},
-                              {0, 1024, 1}, {1, 1024, 1}, {0, 512, 1}, {1, 512, 1}};
+  const GatherCfg cands[10] = {{0, 256, 0},  {1, 256, 0},  {0, 128, 0}, {1, 128, 0}, {2, 128, 0},
+                               {2, 256, 0},  {0, 1024, 1}, {1, 1024, 1}, {0, 512, 1}, {1, 512, 1}};
   const GatherCfg acands[3] = {{0, 256, 0}, {0, 1024, 1}, {0, 512, 1}};
   // time one solve (after one untimed run) for every candidate; keep the fastest
   auto pick = [&](const char* what, auto&& run, GatherCfg& best, bool aop = false) -> int {
     float tbest = 1e30f;
-    const int ncand = aop ? 3 : 8;
+    const int ncand = aop ? 3 : 10;
     for (int ic = 0; ic < ncand; ++ic) {
       const GatherCfg& g = aop ? acands[ic] : cands[ic];
       run(g);
