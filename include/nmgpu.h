@@ -111,7 +111,9 @@ typedef struct {
                          < 0 off                                               */
   double resid_tol;   /* adaptive refinement target for err_ref (0: 1e-10)        */
   int refine_sweeps;  /* adaptive refinement: at most this many passes, each
-                         closed by an FP64 Rayleigh-Ritz (0: 2)                 */
+                         closed by an FP64 Rayleigh-Ritz (0: until the wanted
+                         Ritz vectors meet resid_tol, at most 6, stopping when
+                         a pass no longer halves their largest residual)     */
   int refine_maxdeg;  /* adaptive refinement: degree cap per block (0: 4000)      */
   double refine_band; /* adaptive refinement: the damped band starts at this
                          multiple of the block's largest Ritz value (0: 8)     */
@@ -121,6 +123,16 @@ typedef struct {
                          -1 without it                                          */
   nm_progress_fn progress; /* host callback at phase boundaries (NULL: none)      */
   void* progress_data;     /* first argument of progress                          */
+  double refine_guard; /* adaptive refinement: the Ritz vectors with Rayleigh
+                          quotients in (b, g b] and [a / g, a) join the
+                          refinement and every Rayleigh-Ritz pass as guards
+                          (then dropped), g = this (0: 1.3; <= 1: no guards)  */
+  double refine_near;  /* adaptive refinement passes after the first: the damped
+                          band starts at this multiple of the largest guarded
+                          Ritz value, or higher where the polynomial would grow
+                          by more than refine_growth below a block's Ritz
+                          values (0: 1.05; < 0: every pass uses refine_band)  */
+  double refine_growth; /* see refine_near (0: 1e3)                             */
 } nm_solve_opts;
 
 typedef struct {
@@ -147,6 +159,8 @@ typedef struct {
   int refine_maxdeg;     /* largest refinement degree                               */
   long long refine_steps;      /* block degree steps spent refining                 */
   double res2_before_refine;   /* largest res2 of the Ritz vectors before refining  */
+  int refine_guards;     /* guard Ritz vectors (quotients just outside [a, b]) that
+                            took part in the refinement                          */
 } nm_result;
 
 typedef struct nm_ctx nm_ctx;

@@ -45,6 +45,7 @@ module nmgpu_mod
     integer(c_int) :: refine_purge
     type(c_funptr) :: progress
     type(c_ptr) :: progress_data
+    real(c_double) :: refine_guard, refine_near, refine_growth
   end type nm_solve_opts
 
   type, bind(C) :: nm_result
@@ -60,6 +61,7 @@ module nmgpu_mod
     integer(c_int) :: refine_passes, refine_blocks, refine_maxdeg
     integer(c_long_long) :: refine_steps
     real(c_double) :: res2_before_refine
+    integer(c_int) :: refine_guards
   end type nm_result
 
   type, bind(C) :: nm_slice

@@ -37,6 +37,10 @@ def main(argv=None) -> None:
     ap.add_argument("--refine-maxdeg", type=int, default=0)
     ap.add_argument("--refine-band", type=float, default=0.0)
     ap.add_argument("--refine-purge", type=int, default=0, help="0 auto, 1 every block, -1 none")
+    ap.add_argument("--refine-guard", type=float, default=0.0, help="guard range factor g (0: 1.3; <= 1: none)")
+    ap.add_argument("--refine-growth", type=float, default=0.0, help="near passes: growth bound (0: 1e3)")
+    ap.add_argument("--refine-near", type=float, default=0.0,
+                    help="later passes: band from this x the top guarded Ritz value (0: 1.05; < 0: band passes)")
     ap.add_argument("--skip-fp64", action="store_true", help="mixed path only (no comparison)")
     ap.add_argument("--orth", type=int, default=0,
                     help="mixed Gram-Schmidt: 0 tensor-core projection, 1 FP64, 2 cuBLAS SGEMM")
@@ -51,7 +55,9 @@ def main(argv=None) -> None:
     lo, hi = a.interval
     out = {"cells": a.cells, "porder": a.porder, "lateral": a.lateral, "interval_mhz": [lo, hi], "polish": a.polish,
            "gravity": a.gravity, "inner_tol": a.inner_tol, "resid_tol": a.resid_tol,
-           "refine_sweeps": a.refine_sweeps, "refine_maxdeg": a.refine_maxdeg, "refine_band": a.refine_band, "refine_purge": a.refine_purge}
+           "refine_sweeps": a.refine_sweeps, "refine_maxdeg": a.refine_maxdeg, "refine_band": a.refine_band, "refine_purge": a.refine_purge,
+           "refine_guard": a.refine_guard, "refine_near": a.refine_near,
+           "refine_growth": a.refine_growth}
     res = {}
     runs = [("mixed", NM_PREC_MIXED, 32)] + ([] if (a.fp64_lam or a.skip_fp64) else
                                               [("fp64", NM_PREC_FP64, a.fp64_block)])
@@ -60,7 +66,8 @@ def main(argv=None) -> None:
             t = time.perf_counter()
             kw = dict(polish=a.polish, resid_tol=a.resid_tol, refine_sweeps=a.refine_sweeps,
                       refine_maxdeg=a.refine_maxdeg, refine_band=a.refine_band,
-                      refine_purge=a.refine_purge) if name == "mixed" else {}
+                      refine_purge=a.refine_purge, refine_guard=a.refine_guard,
+                      refine_near=a.refine_near, refine_growth=a.refine_growth) if name == "mixed" else {}
             r = sv.solve(lo, hi, block=block, want_vectors=False, **kw)
             dt = time.perf_counter() - t
         res[name] = r
@@ -72,7 +79,8 @@ def main(argv=None) -> None:
                      "res2_median": float(np.median(r.res2)) if len(r.lam) else None,
                      "gated_1e-10": int((r.err_ref <= 1e-10).sum()),
                      "refinement": {k: r.counts[k] for k in ("refine_passes", "refine_blocks", "refine_maxdeg",
-                                                             "refine_steps", "res2_before_refine")}}
+                                                             "refine_steps", "res2_before_refine",
+                                                             "refine_guards")}}
     m = res["mixed"].lam
     if a.skip_fp64 and not a.fp64_lam:
         print(json.dumps(out))

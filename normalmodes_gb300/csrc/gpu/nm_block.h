@@ -192,9 +192,14 @@ int block_time_op(nm_ctx* c, int which, int reps, double* ms, double* bytes, int
 int block_build(nm_ctx* c, const nm_csr* A, const nm_csr* B, const nm_csr* Ap, const nm_csr* E, const nm_csr* ET);
 void block_free(nm_ctx* c);
 // Block filtered Lanczos; on success U (n x nc, column-major, device, owned
-// by the caller) holds the Ritz vectors with p(theta) >= bar.
+// by the caller) holds the Ritz vectors with p(theta) >= bar, and, when
+// 0 < guard_bar < bar, up to max_guard (-1: half the count above the bar
+// plus 64) more with the largest filter values in [guard_bar, bar): the
+// Ritz vectors of the modes just outside [a, b].
 int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double** U, int* nc, int* steps,
-                  double* t_filter, double* t_orth, double* t_eig);
+                  double* t_filter, double* t_orth, double* t_eig, double guard_bar = -1.0, int max_guard = -1);
+// Value of the filter polynomial p at x (the Chebyshev series of pol).
+double filter_value(const Pol& pol, double x);
 // FP64 Rayleigh-Ritz on the columns of U (n x nc): U <- U Q with
 // (U^T A U) Q = (U^T B U) Q Theta.  Resolves the mixing of close Ritz pairs
 // left by an FP32 filter.
@@ -265,18 +270,35 @@ int polish64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
 // two large FP32 terms cancel; purge < 0: h = T_d(l(x)) / T_d(l(theta)).
 struct RefineParams {
   double tol_res2 = 1e-7;  // target ||A u - theta B u||_2 / (|theta| ||u||_B)
-  double band = 8.0;
+  double band = 8.0;       // damped band from band x the block's largest Ritz value ...
+  double near_c = 0.0;     // ... or, if > 0, from near_c, moved up as far as needed
+  double max_growth = 1e3; // to keep the growth below the Ritz values under this
   double safety = 4.0;
   int purge = 0;
   int mindeg = 8, maxdeg = 4000;
+  // Ritz values outside [want_lo, want_hi] are guards: their target is
+  // guard_tol x tol_res2
+  double want_lo = 0.0, want_hi = 1e300, guard_tol = 100.0;
 };
 struct RefineStats {
   int blocks = 0, max_deg = 0;   // blocks refined, largest degree
   long long steps = 0;           // block degree steps spent
   double max_res2_before = 0.0;  // largest res2 measured before the pass
+  double max_res2_want = 0.0;    // ... of the Ritz values in [want_lo, want_hi]
+  int want_above = 0;            // of those, above the target
 };
 int refine_block_degree(const std::vector<double>& theta, const std::vector<double>& res2, double c0, double lmax,
                         const RefineParams& rp, bool purge);
+// log of the largest growth factor T_d(l(x)) / T_d(l(theta_j)), x in [0,
+// theta_j), of the block's refinement polynomial (degree from
+// refine_block_degree) over its Ritz values theta_j
+double refine_log_growth(const std::vector<double>& theta, const std::vector<double>& res2, double c0, double lmax,
+                         const RefineParams& rp, bool purge);
+// start of the damped band of one block: band x thmax, or for a near pass
+// the lowest c >= max(near_c, 1.05 thmax) with refine_log_growth <=
+// log(max_growth) (never above band x thmax), capped at lmax / 2
+double refine_band_start(const std::vector<double>& theta, const std::vector<double>& res2, double thmax, double lmax,
+                         const RefineParams& rp, bool purge);
 int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, const RefineParams& rp,
              RefineStats* stats);
 

@@ -266,9 +266,9 @@ int cheb_degree_for(const ChebSetup& ref, double eps) {
   return std::max(1, std::min(ref.deg, d));
 }
 
-// p(0) of a filter polynomial: sum_k mu_k T_k(-cc/dd).
-double filter_at_zero(const Pol& pol) {
-  const double l0 = -pol.cc / pol.dd;
+// p(x) of a filter polynomial: sum_k mu_k T_k((x - cc) / dd).
+double filter_value(const Pol& pol, double x) {
+  const double l0 = (x - pol.cc) / pol.dd;
   double tkm1 = 1.0, tk = l0, p0 = pol.mu.empty() ? 0.0 : pol.mu[0];
   for (int k = 1; k <= pol.deg; ++k) {
     p0 += pol.mu[k] * tk;
@@ -278,6 +278,8 @@ double filter_at_zero(const Pol& pol) {
   }
   return p0;
 }
+
+double filter_at_zero(const Pol& pol) { return filter_value(pol, 0.0); }
 
 PolishPlan polish_plan(const double xintv[4], int requested) {
   PolishPlan p;
@@ -577,7 +579,7 @@ int ensure32(nm_ctx* c, Basis32& b, int n, int ncols) {
 }  // namespace
 
 int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double** Uout, int* ncout, int* steps_out,
-                  double* t_filter, double* t_orth, double* t_eig) {
+                  double* t_filter, double* t_orth, double* t_eig, double guard_bar, int max_guard) {
   BlockState* st = bs(c);
   if (!st || !st->ok) return set_err(c, NM_ERR_ARG, "block mode needs the 3-component operator structure");
   const int n = c->n, np = c->np, S = kBlk;
@@ -982,6 +984,13 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
       first = i;
       break;
     }
+  if (guard_bar > 0.0 && guard_bar < pol.bar && first < K) {
+    // guards: the next Ritz values below the bar, largest filter value first
+    const int cap = max_guard >= 0 ? max_guard : (K - first) / 2 + 64;
+    int g0 = first;
+    while (g0 > 0 && first - g0 < cap && evals[g0 - 1] >= guard_bar) --g0;
+    first = g0;
+  }
   const int nc = K - first;
   double* U = nullptr;
   if (nc > 0) {
@@ -1365,16 +1374,47 @@ int refine_block_degree(const std::vector<double>& theta, const std::vector<doub
                         const RefineParams& rp, bool purge) {
   double need = 0.0;
   for (size_t j = 0; j < theta.size() && j < res2.size(); ++j) {
-    if (!(res2[j] > rp.tol_res2) || !(theta[j] > 0.0)) continue;
-    // the closing (B~^-1 A) / theta step multiplies the band's components by
-    // up to lmax / theta: the damping has to cover that too
-    const double damp = rp.safety * (purge ? lmax / theta[j] : 1.0) * res2[j] / rp.tol_res2;
+    const double tol = rp.tol_res2 * (theta[j] < rp.want_lo || theta[j] > rp.want_hi ? rp.guard_tol : 1.0);
+    if (!(res2[j] > tol) || !(theta[j] > 0.0)) continue;
+    // the x / theta factor multiplies the band's components by up to
+    // lmax / theta: the damping has to cover that too
+    const double damp = rp.safety * (purge ? lmax / theta[j] : 1.0) * res2[j] / tol;
     const double delta = 2.0 * (c0 - theta[j]) / (lmax - c0);
     if (!(delta > 0.0)) continue;  // at or above the band: not refinable
     need = std::max(need, std::acosh(damp) / std::acosh(1.0 + delta));
   }
   if (need <= 0.0) return 0;
   return std::max(rp.mindeg, std::min(rp.maxdeg, (int)std::ceil(need)));
+}
+
+double refine_log_growth(const std::vector<double>& theta, const std::vector<double>& res2, double c0, double lmax,
+                         const RefineParams& rp, bool purge) {
+  const int d = refine_block_degree(theta, res2, c0, lmax, rp, purge);
+  if (d <= 0 || !(lmax > c0)) return 0.0;
+  // T_d(l(x)) = cosh(d acosh(|l(x)|)) below the band; the ratio's log is
+  // d (acosh(l(0)) - acosh(l(theta))) to within log 2
+  const double a0 = std::acosh(1.0 + 2.0 * c0 / (lmax - c0));
+  double g = 0.0;
+  for (double t : theta)
+    if (t > 0.0 && t < c0) g = std::max(g, d * (a0 - std::acosh(1.0 + 2.0 * (c0 - t) / (lmax - c0))));
+  return g;
+}
+
+double refine_band_start(const std::vector<double>& theta, const std::vector<double>& res2, double thmax, double lmax,
+                         const RefineParams& rp, bool purge) {
+  const double cap = 0.5 * lmax;
+  const double far = std::min(rp.band * thmax, cap);
+  if (!(rp.near_c > 0.0)) return far;
+  double lo = std::min(std::max(rp.near_c, 1.05 * thmax), cap);
+  const double lim = std::log(rp.max_growth);
+  if (lo >= far || refine_log_growth(theta, res2, lo, lmax, rp, purge) <= lim) return lo;
+  double hi = far;
+  if (refine_log_growth(theta, res2, hi, lmax, rp, purge) > lim) return hi;
+  for (int it = 0; it < 48; ++it) {  // the growth falls as the band moves up
+    const double mid = 0.5 * (lo + hi);
+    (refine_log_growth(theta, res2, mid, lmax, rp, purge) > lim ? lo : hi) = mid;
+  }
+  return hi;
 }
 
 int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, const RefineParams& rp,
@@ -1456,10 +1496,14 @@ int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, dou
       thmax = std::max(thmax, th[col]);
       if (th[col] > 0.0) thmin = thmin > 0.0 ? std::min(thmin, th[col]) : th[col];
       worst = std::max(worst, rb[col]);
+      if (th[col] >= rp.want_lo && th[col] <= rp.want_hi) {
+        stats.max_res2_want = std::max(stats.max_res2_want, rb[col]);
+        stats.want_above += rb[col] > rp.tol_res2;
+      }
     }
     stats.max_res2_before = std::max(stats.max_res2_before, worst);
-    const double c0 = std::min(rp.band * thmax, 0.5 * lmax);
     const bool purge = rp.purge >= 0 && thmin > 0.0;
+    const double c0 = refine_band_start(tb, rb, thmax, lmax, rp, purge);
     // One pass of U <- h(B~^-1 A) U in correction form, driven by the FP64
     // residual R (in sAU / sBU), all vectors FP32:
     //  * damping only (no purge), h = T_d(l(x)) / T_d(l(theta)):
@@ -1589,6 +1633,25 @@ int nm_test_cheb_degree(double lmin, double lmax, int ref_deg, double eps) {
 double nm_test_filter_at_zero(const double* xintv, double thresh_int, double thresh_ext, int damping) {
   const nmg::Pol P = nmg::find_pol(xintv, thresh_int, thresh_ext, 2, 10000, damping);
   return nmg::filter_at_zero(P);
+}
+// adaptive refinement of one block (purge form): out = {band start c0,
+// degree, log growth}; near_c <= 0 for a first (band 8) pass
+void nm_test_refine_band(const double* theta, const double* res2, int n, double lmax, double tol_res2, double near_c,
+                         double* out) {
+  nmg::RefineParams rp;
+  rp.tol_res2 = tol_res2;
+  rp.near_c = near_c;
+  std::vector<double> t(theta, theta + n), r(res2, res2 + n);
+  double thmax = 0.0;
+  for (double x : t) thmax = std::max(thmax, x);
+  const double c0 = nmg::refine_band_start(t, r, thmax, lmax, rp, true);
+  out[0] = c0;
+  out[1] = nmg::refine_block_degree(t, r, c0, lmax, rp, true);
+  out[2] = nmg::refine_log_growth(t, r, c0, lmax, rp, true);
+}
+// p(x) of the filter find_pol designs for xintv
+double nm_test_filter_value(const double* xintv, double thresh_int, double thresh_ext, int damping, double x) {
+  return nmg::filter_value(nmg::find_pol(xintv, thresh_int, thresh_ext, 2, 10000, damping), x);
 }
 // refinement plan: out = {deg, refine}, band = {cfrac, bfloor}
 void nm_test_polish_plan(const double* xintv, int requested, int* out, double* band) {

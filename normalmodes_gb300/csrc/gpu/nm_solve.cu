@@ -423,8 +423,19 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
   if (o.block > 1) {
     converged = true;
     int steps = 0;
+    // adaptive refinement of the mixed path: guard Ritz vectors of the modes
+    // just outside [a, b] (filter value down to that at g b and a / g)
+    const bool adaptive = mixed && o.polish == 0;
+    const double gfac = o.refine_guard == 0.0 ? 1.3 : o.refine_guard;
+    const bool guards = adaptive && gfac > 1.0;
+    double guard_bar = -1.0;
+    if (guards) {
+      guard_bar = filter_value(pol, std::min(gfac * xintv[1], xintv[3]));
+      if (xintv[0] > xintv[2]) guard_bar = std::min(guard_bar, filter_value(pol, std::max(xintv[0] / gfac, xintv[2])));
+      if (!(guard_bar > 0.0)) guard_bar = -1.0;
+    }
     if ((rc = block_lanczos(c, pol, maxit, o.use_graph != 0, &U, &nc, &steps, &res->t_filter, &res->t_orth,
-                            &res->t_eig)))
+                            &res->t_eig, guard_bar)))
       return rc;
     // FP32 filter: close Ritz pairs are mixed at the FP32 noise level; an
     // FP64 Rayleigh-Ritz over the Ritz block separates them.
@@ -459,13 +470,42 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
         return rc;
       }
       progress(c, NM_PHASE_RITZ, nc, nc);
+      if (refine && guards) {
+        // keep the Ritz vectors with quotients in [a / g, g b] (ascending
+        // after the Rayleigh-Ritz); the rest of the filter's tail goes
+        int i0 = 0, i1 = nc;
+        while (i0 < nc && theta[i0] < xintv[0] / gfac) ++i0;
+        while (i1 > i0 && theta[i1 - 1] > gfac * xintv[1]) --i1;
+        if (i0 > 0)
+          for (int j = i0; j < i1; ++j)
+            NM_CUDA(c, cudaMemcpyAsync(U + (size_t)(j - i0) * n, U + (size_t)j * n, sizeof(double) * n,
+                                       cudaMemcpyDeviceToDevice, c->stream));
+        theta = std::vector<double>(theta.begin() + i0, theta.begin() + i1);
+        nc = i1 - i0;
+        res->refine_guards = 0;
+        for (double t : theta) res->refine_guards += t < xintv[0] || t > xintv[1];
+      }
       RefineParams rp;
-      rp.tol_res2 = (o.resid_tol > 0 ? o.resid_tol : 1e-10) * std::sqrt((double)n);  // err_ref = res2 / sqrt(N)
+      // err_ref = res2 / sqrt(N); the passes aim at half the target, so the
+      // closing Rayleigh-Ritz cannot lift a pair back over it
+      rp.tol_res2 = 0.5 * (o.resid_tol > 0 ? o.resid_tol : 1e-10) * std::sqrt((double)n);
       if (o.refine_maxdeg > 0) rp.maxdeg = o.refine_maxdeg;
       if (o.refine_band > 1.0) rp.band = o.refine_band;
       rp.purge = o.refine_purge;
-      const int sweeps = o.refine_sweeps > 0 ? o.refine_sweeps : 2;
+      if (o.refine_growth > 1.0) rp.max_growth = o.refine_growth;
+      rp.want_lo = xintv[0];
+      rp.want_hi = xintv[1];
+      const double nearf = o.refine_near == 0.0 ? 1.05 : o.refine_near;
+      // refine_sweeps 0: passes until every wanted Ritz vector meets the
+      // target, at most 6, stopping early when a pass no longer halves the
+      // largest wanted residual
+      const int sweeps = o.refine_sweeps > 0 ? o.refine_sweeps : 6;
+      double prev_want = 0.0;
       for (int sw = 0; refine && sw < sweeps; ++sw) {
+        // the first pass damps from band x the block's top (the FP32
+        // filter's noise far up the spectrum); the later ones from just above
+        // the guarded set, so the out-of-set modes next to b are damped too
+        rp.near_c = sw > 0 && nearf > 0.0 && !theta.empty() ? nearf * theta.back() : 0.0;
         RefineStats rs;
         if ((rc = refine64(c, U, nc, theta, res->xintv[3], rp, &rs))) {
           cudaFree(U);
@@ -484,6 +524,9 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
           return rc;
         }
         ++res->refine_passes;
+        // residuals measured before this pass against those before the last
+        if (o.refine_sweeps <= 0 && sw >= 2 && !(rs.max_res2_want < 0.5 * prev_want)) break;
+        prev_want = rs.max_res2_want;
       }
     }
     res->lanczos_steps = steps;

@@ -52,7 +52,8 @@ class NmSolveOpts(C.Structure):
                 ("want_vectors", C.c_int), ("unscale", C.c_int), ("use_graph", C.c_int), ("block", C.c_int),
                 ("polish", C.c_int), ("resid_tol", C.c_double), ("refine_sweeps", C.c_int),
                 ("refine_maxdeg", C.c_int), ("refine_band", C.c_double), ("refine_purge", C.c_int),
-                ("progress", C.c_void_p), ("progress_data", C.c_void_p)]
+                ("progress", C.c_void_p), ("progress_data", C.c_void_p), ("refine_guard", C.c_double),
+                ("refine_near", C.c_double), ("refine_growth", C.c_double)]
 
 
 # void (*)(void* data, int phase, int done, int total)
@@ -70,7 +71,8 @@ class NmResult(C.Structure):
                 ("n_amv", C.c_longlong), ("n_bsolve", C.c_longlong), ("n_spmv", C.c_longlong),
                 ("n_kernels", C.c_longlong), ("t_filter", C.c_double), ("t_orth", C.c_double),
                 ("t_eig", C.c_double), ("refine_passes", C.c_int), ("refine_blocks", C.c_int),
-                ("refine_maxdeg", C.c_int), ("refine_steps", C.c_longlong), ("res2_before_refine", C.c_double)]
+                ("refine_maxdeg", C.c_int), ("refine_steps", C.c_longlong), ("res2_before_refine", C.c_double),
+                ("refine_guards", C.c_int)]
 
 
 class NmElemModel(C.Structure):
@@ -226,6 +228,9 @@ def lib() -> C.CDLL:
         L.nm_test_filter_at_zero.argtypes = [dp, C.c_double, C.c_double, C.c_int]
         L.nm_test_filter_at_zero.restype = C.c_double
         L.nm_test_polish_plan.argtypes = [dp, C.c_int, C.POINTER(C.c_int), dp]
+        L.nm_test_refine_band.argtypes = [dp, dp, C.c_int, C.c_double, C.c_double, C.c_double, dp]
+        L.nm_test_filter_value.argtypes = [dp, C.c_double, C.c_double, C.c_int, C.c_double]
+        L.nm_test_filter_value.restype = C.c_double
         L.nm_test_polish_block.argtypes = [dp, C.c_int, C.c_double, C.c_double, dp]
         L.nm_test_polish_block.restype = C.c_int
         L.nm_solve_batched.argtypes = [vp, C.POINTER(NmSlice), C.c_int, C.POINTER(NmSolveOpts), C.POINTER(NmResult)]
@@ -379,7 +384,8 @@ class Solver:
     @staticmethod
     def _solve_opts(maxit=0, tol=0.0, ab_bounds=None, want_vectors=True, unscale=False, use_graph=True, damping=1,
                     mlan_bounds=0, block=0, polish=0, resid_tol=0.0, refine_sweeps=0, refine_maxdeg=0,
-                    progress=None, refine_band=0.0, refine_purge=0) -> "NmSolveOpts":
+                    progress=None, refine_band=0.0, refine_purge=0, refine_guard=0.0,
+                    refine_near=0.0, refine_growth=0.0) -> "NmSolveOpts":
         o = NmSolveOpts()
         lib().nm_default_solve_opts(C.byref(o))
         o.resid_tol = resid_tol
@@ -387,6 +393,9 @@ class Solver:
         o.refine_maxdeg = refine_maxdeg
         o.refine_band = refine_band
         o.refine_purge = refine_purge
+        o.refine_guard = refine_guard
+        o.refine_near = refine_near
+        o.refine_growth = refine_growth
         if progress is not None:  # an NM_PROGRESS_FN the caller keeps alive for the call
             o.progress = C.cast(progress, C.c_void_p)
         o.maxit = maxit
@@ -417,13 +426,14 @@ class Solver:
                            {"amv": r.n_amv, "bsolve": r.n_bsolve, "spmv": r.n_spmv, "kernels": r.n_kernels,
                             "refine_passes": r.refine_passes, "refine_blocks": r.refine_blocks,
                             "refine_maxdeg": r.refine_maxdeg, "refine_steps": r.refine_steps,
-                            "res2_before_refine": r.res2_before_refine})
+                            "res2_before_refine": r.res2_before_refine, "refine_guards": r.refine_guards})
 
     def solve(self, lowfreq: float, upfreq: float, maxit: int = 0, tol: float = 0.0, ab_bounds=None,
               want_vectors: bool = True, unscale: bool = False, use_graph: bool = True, damping: int = 1,
               mlan_bounds: int = 0, allow_noconv: bool = False, block: int = 0, polish: int = 0,
               resid_tol: float = 0.0, refine_sweeps: int = 0, refine_maxdeg: int = 0,
-              progress=None, refine_band: float = 0.0, refine_purge: int = 0) -> SolveResult:
+              progress=None, refine_band: float = 0.0, refine_purge: int = 0, refine_guard: float = 0.0,
+              refine_near: float = 0.0, refine_growth: float = 0.0) -> SolveResult:
         """nm_solve on [lowfreq, upfreq] mHz.  `progress`, if given, is a
         Python callable progress(phase, done, total) called at the solve's
         phase and block boundaries (NM_PHASE_*), stream drained."""
@@ -432,7 +442,8 @@ class Solver:
         if progress is not None:
             cb = NM_PROGRESS_FN(lambda _d, ph, done, tot: progress(ph, done, tot))
         o = self._solve_opts(maxit, tol, ab_bounds, want_vectors, unscale, use_graph, damping, mlan_bounds, block,
-                             polish, resid_tol, refine_sweeps, refine_maxdeg, cb, refine_band, refine_purge)
+                             polish, resid_tol, refine_sweeps, refine_maxdeg, cb, refine_band, refine_purge,
+                             refine_guard, refine_near, refine_growth)
         r = NmResult()
         rc = L.nm_solve(self._h, lowfreq, upfreq, C.byref(o), C.byref(r))
         try:

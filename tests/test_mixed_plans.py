@@ -85,3 +85,74 @@ def test_refinement_plan_narrow_spectrum_and_off():
     # off on request, and when the band would start in the upper half
     assert _plan([a, b, 0.0, lmax], -1)[:2] == (0, False)
     assert _plan([1e-3, 0.4, 0.0, 1.0], 0)[1] is False
+
+
+def _refine_band(theta, res2, lmax, tol, near_c):
+    t = np.ascontiguousarray(theta, dtype=np.float64)
+    r = np.ascontiguousarray(res2, dtype=np.float64)
+    out = np.zeros(3)
+    nmgpu.lib().nm_test_refine_band(_dp(t), _dp(r), len(t), lmax, tol, near_c, _dp(out))
+    return out[0], int(out[1]), out[2]
+
+
+def _degree(theta, res2, c, lmax, tol):
+    need = 0.0
+    for t, r in zip(theta, res2):
+        if r > tol:
+            need = max(need, math.acosh(4.0 * (lmax / t) * r / tol) / math.acosh(1 + 2 * (c - t) / (lmax - c)))
+    return 0 if need == 0 else max(8, min(4000, math.ceil(need)))
+
+
+def _growth(theta, c, lmax, d):
+    a0 = math.acosh(1 + 2 * c / (lmax - c))
+    return max(d * (a0 - math.acosh(1 + 2 * (c - t) / (lmax - c))) for t in theta)
+
+
+# a block of 32 Ritz values of a 1.2M-DOF-like spectrum (lmax / b ~ 1e3)
+_TH = np.linspace(1.0e-4, 1.5e-4, 32)
+_LMAX = 0.2
+
+
+@pytest.mark.parametrize("res2", [1e-3, 1e-6, 3e-8])
+def test_refinement_first_pass_band(res2):
+    """First pass: the damped band starts at 8 x the block's top Ritz value
+    (lmax / 2 at most); the degree is the largest over the block of
+    acosh(4 (lmax / theta) res2 / tol) / acosh(1 + 2 (c - theta) / (lmax - c))."""
+    r = np.full(32, res2)
+    tol = 1e-10 * math.sqrt(1.2e6)
+    c, d, g = _refine_band(_TH, r, _LMAX, tol, 0.0)
+    assert c == pytest.approx(8 * _TH.max(), rel=1e-15)
+    assert d == _degree(_TH, r, c, _LMAX, tol)
+    if d:
+        assert g == pytest.approx(_growth(_TH, c, _LMAX, d), rel=1e-12)
+
+
+@pytest.mark.parametrize("res2,near", [(1e-6, 1.05 * 1.3 * 1.5e-4), (1e-3, 1.05 * 1.3 * 1.5e-4), (1e-7, 1.6e-4)])
+def test_refinement_near_pass_band_bounds_growth(res2, near):
+    """Later passes: the band starts at near_c (or 1.05 x the block's top),
+    moved up only as far as needed to keep the growth below the Ritz
+    values, d (acosh l(0) - acosh l(theta)), under log 1e3."""
+    r = np.full(32, res2)
+    tol = 1e-10 * math.sqrt(1.2e6)
+    c, d, g = _refine_band(_TH, r, _LMAX, tol, near)
+    lo = max(near, 1.05 * _TH.max())
+    assert lo <= c <= 8 * _TH.max()
+    assert d == _degree(_TH, r, c, _LMAX, tol)
+    assert g == pytest.approx(_growth(_TH, c, _LMAX, d), rel=1e-12)
+    lim = math.log(1e3)
+    if c > lo * (1 + 1e-12):
+        assert g <= lim + 1e-9
+        c2 = c * (1 - 1e-6)
+        assert _growth(_TH, c2, _LMAX, _degree(_TH, r, c2, _LMAX, tol)) > lim - 1e-3
+    else:
+        assert g <= lim + 1e-9
+
+
+def test_filter_value_matches_chebyshev_series():
+    xintv = [3.9e-7, 1.58e-4, -1e-8, 0.6]
+    x = np.array(xintv)
+    p = O.find_pol(xintv, 0.8, 0.7, 2, 10000, 1)
+    for lam in (0.0, 1e-5, 1.58e-4, 1.3 * 1.58e-4, 0.3):
+        ref = np.polynomial.chebyshev.chebval((lam - p.cc) / p.dd, p.mu)
+        got = nmgpu.lib().nm_test_filter_value(_dp(x), 0.8, 0.7, 1, lam)
+        assert abs(got - ref) <= 1e-12 * max(1.0, abs(ref))
