@@ -443,7 +443,8 @@ def main():
                    "max_res2": float(res.res2.max()) if nev else None,
                    "median_res2": float(np.median(res.res2)) if nev else None,
                    "refinement": {k: res.counts[k] for k in ("refine_passes", "refine_blocks", "refine_maxdeg",
-                                                             "refine_steps", "res2_before_refine")},
+                                                             "refine_steps", "res2_before_refine",
+                                                             "refine_guards")},
                    "parallelism": f"replicas x{ws}", "autotuned_gathers": tuned},
         "gpu_launches": res.counts["kernels"],
         "clocks": clocks,

@@ -126,7 +126,7 @@ typedef struct {
   double refine_guard; /* adaptive refinement: the Ritz vectors with Rayleigh
                           quotients in (b, g b] and [a / g, a) join the
                           refinement and every Rayleigh-Ritz pass as guards
-                          (then dropped), g = this (0: 1.3; <= 1: no guards)  */
+                          (then dropped), g = this (0: 1.5; <= 1: no guards)  */
   double refine_near;  /* adaptive refinement passes after the first: the damped
                           band starts at this multiple of the largest guarded
                           Ritz value, or higher where the polynomial would grow

@@ -29,6 +29,7 @@ def main(argv=None) -> None:
     ap.add_argument("--polish", type=int, default=0, help="mixed path refinement degree (0: default, <0: off)")
     ap.add_argument("--fp64-lam", default=None, help="eigenvalues of an earlier FP64 solve (.npy) instead of solving")
     ap.add_argument("--save-fp64-lam", default=None, help="write the FP64 eigenvalues to this .npy file")
+    ap.add_argument("--save-mixed-lam", default=None, help="write the mixed-path eigenvalues to this .npy file")
     ap.add_argument("--gravity", action="store_true", help="operators with the reference gravity (JOB = 2)")
     ap.add_argument("--inner-tol", type=float, default=0.0,
                     help="mixed path: accuracy of the FP32 filter's inner B^-1 solve (0: 2^-24)")
@@ -37,7 +38,7 @@ def main(argv=None) -> None:
     ap.add_argument("--refine-maxdeg", type=int, default=0)
     ap.add_argument("--refine-band", type=float, default=0.0)
     ap.add_argument("--refine-purge", type=int, default=0, help="0 auto, 1 every block, -1 none")
-    ap.add_argument("--refine-guard", type=float, default=0.0, help="guard range factor g (0: 1.3; <= 1: none)")
+    ap.add_argument("--refine-guard", type=float, default=0.0, help="guard range factor g (0: 1.5; <= 1: none)")
     ap.add_argument("--refine-growth", type=float, default=0.0, help="near passes: growth bound (0: 1e3)")
     ap.add_argument("--refine-near", type=float, default=0.0,
                     help="later passes: band from this x the top guarded Ritz value (0: 1.05; < 0: band passes)")
@@ -72,7 +73,7 @@ def main(argv=None) -> None:
             dt = time.perf_counter() - t
         res[name] = r
         out[name] = {"nev": len(r.lam), "seconds": round(dt, 3), "block": block, "lanczos_vectors": r.lanczos_steps,
-                     "filter_degree": r.pol_deg,
+                     "filter_degree": r.pol_deg, "times_s": {k: round(v, 3) for k, v in r.times.items()},
                      "err_ref_max": float(r.err_ref.max()) if len(r.lam) else None,
                      "err_ref_median": float(np.median(r.err_ref)) if len(r.lam) else None,
                      "res2_max": float(r.res2.max()) if len(r.lam) else None,
@@ -88,6 +89,8 @@ def main(argv=None) -> None:
     f = np.load(a.fp64_lam) if a.fp64_lam else res["fp64"].lam
     if a.save_fp64_lam and "fp64" in res:
         np.save(a.save_fp64_lam, f)
+    if a.save_mixed_lam:
+        np.save(a.save_mixed_lam, res["mixed"].lam)
     out["same_count"] = len(m) == len(f)
     if len(m) == len(f) and len(f):
         rel = np.abs(m - f) / np.abs(f)

@@ -272,7 +272,9 @@ struct RefineParams {
   double tol_res2 = 1e-7;  // target ||A u - theta B u||_2 / (|theta| ||u||_B)
   double band = 8.0;       // damped band from band x the block's largest Ritz value ...
   double near_c = 0.0;     // ... or, if > 0, from near_c, moved up as far as needed
-  double max_growth = 1e3; // to keep the growth below the Ritz values under this
+  double max_growth = 1e3; // to keep the growth below the Ritz values under this,
+  double low_x = 0.0;      // and that of modes in (0, low_x] (out of the set below
+  double max_low_growth = 2.0;  // its lowest Ritz value), x / theta included, under this
   double safety = 4.0;
   int purge = 0;
   int mindeg = 8, maxdeg = 4000;
@@ -294,9 +296,15 @@ int refine_block_degree(const std::vector<double>& theta, const std::vector<doub
 // refine_block_degree) over its Ritz values theta_j
 double refine_log_growth(const std::vector<double>& theta, const std::vector<double>& res2, double c0, double lmax,
                          const RefineParams& rp, bool purge);
+// log of the largest gain (x / theta_j) T_d(l(x)) / T_d(l(theta_j)) of the
+// block's refinement polynomial over x in (0, rp.low_x]: modes below the
+// refined set, which no Rayleigh-Ritz removes (-inf without low_x)
+double refine_low_growth(const std::vector<double>& theta, const std::vector<double>& res2, double c0, double lmax,
+                         const RefineParams& rp, bool purge);
 // start of the damped band of one block: band x thmax, or for a near pass
 // the lowest c >= max(near_c, 1.05 thmax) with refine_log_growth <=
-// log(max_growth) (never above band x thmax), capped at lmax / 2
+// log(max_growth) and refine_low_growth <= log(max_low_growth) (never above
+// band x thmax), capped at lmax / 2
 double refine_band_start(const std::vector<double>& theta, const std::vector<double>& res2, double thmax, double lmax,
                          const RefineParams& rp, bool purge);
 int refine64(nm_ctx* c, double* U, int nc, const std::vector<double>& theta, double lmax, const RefineParams& rp,

@@ -1400,19 +1400,40 @@ double refine_log_growth(const std::vector<double>& theta, const std::vector<dou
   return g;
 }
 
+double refine_low_growth(const std::vector<double>& theta, const std::vector<double>& res2, double c0, double lmax,
+                         const RefineParams& rp, bool purge) {
+  const int d = refine_block_degree(theta, res2, c0, lmax, rp, purge);
+  if (d <= 0 || !(lmax > c0) || !(rp.low_x > 0.0)) return -1e300;
+  const double w = lmax - c0;
+  double g = -1e300;
+  for (double t : theta) {
+    if (!(t > rp.low_x) || !(t < c0)) continue;
+    const double at = std::acosh(1.0 + 2.0 * (c0 - t) / w);
+    for (int k = 0; k <= 32; ++k) {  // x from low_x down to 1e-8 low_x
+      const double x = rp.low_x * std::pow(10.0, -0.25 * k);
+      g = std::max(g, std::log(x / t) + d * (std::acosh(1.0 + 2.0 * (c0 - x) / w) - at));
+    }
+  }
+  return g;
+}
+
 double refine_band_start(const std::vector<double>& theta, const std::vector<double>& res2, double thmax, double lmax,
                          const RefineParams& rp, bool purge) {
   const double cap = 0.5 * lmax;
   const double far = std::min(rp.band * thmax, cap);
   if (!(rp.near_c > 0.0)) return far;
   double lo = std::min(std::max(rp.near_c, 1.05 * thmax), cap);
-  const double lim = std::log(rp.max_growth);
-  if (lo >= far || refine_log_growth(theta, res2, lo, lmax, rp, purge) <= lim) return lo;
+  const double lim = std::log(rp.max_growth), lim_low = std::log(rp.max_low_growth);
+  auto over = [&](double c0) {
+    return refine_log_growth(theta, res2, c0, lmax, rp, purge) > lim ||
+           refine_low_growth(theta, res2, c0, lmax, rp, purge) > lim_low;
+  };
+  if (lo >= far || !over(lo)) return lo;
   double hi = far;
-  if (refine_log_growth(theta, res2, hi, lmax, rp, purge) > lim) return hi;
-  for (int it = 0; it < 48; ++it) {  // the growth falls as the band moves up
+  if (over(hi)) return hi;
+  for (int it = 0; it < 48; ++it) {  // both growths fall as the band moves up
     const double mid = 0.5 * (lo + hi);
-    (refine_log_growth(theta, res2, mid, lmax, rp, purge) > lim ? lo : hi) = mid;
+    (over(mid) ? lo : hi) = mid;
   }
   return hi;
 }
@@ -1635,12 +1656,13 @@ double nm_test_filter_at_zero(const double* xintv, double thresh_int, double thr
   return nmg::filter_at_zero(P);
 }
 // adaptive refinement of one block (purge form): out = {band start c0,
-// degree, log growth}; near_c <= 0 for a first (band 8) pass
+// degree, log growth, log low growth}; near_c <= 0 for a first (band 8) pass
 void nm_test_refine_band(const double* theta, const double* res2, int n, double lmax, double tol_res2, double near_c,
-                         double* out) {
+                         double low_x, double* out) {
   nmg::RefineParams rp;
   rp.tol_res2 = tol_res2;
   rp.near_c = near_c;
+  rp.low_x = low_x;
   std::vector<double> t(theta, theta + n), r(res2, res2 + n);
   double thmax = 0.0;
   for (double x : t) thmax = std::max(thmax, x);
@@ -1648,6 +1670,7 @@ void nm_test_refine_band(const double* theta, const double* res2, int n, double 
   out[0] = c0;
   out[1] = nmg::refine_block_degree(t, r, c0, lmax, rp, true);
   out[2] = nmg::refine_log_growth(t, r, c0, lmax, rp, true);
+  out[3] = nmg::refine_low_growth(t, r, c0, lmax, rp, true);
 }
 // p(x) of the filter find_pol designs for xintv
 double nm_test_filter_value(const double* xintv, double thresh_int, double thresh_ext, int damping, double x) {

@@ -426,7 +426,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
     // adaptive refinement of the mixed path: guard Ritz vectors of the modes
     // just outside [a, b] (filter value down to that at g b and a / g)
     const bool adaptive = mixed && o.polish == 0;
-    const double gfac = o.refine_guard == 0.0 ? 1.3 : o.refine_guard;
+    const double gfac = o.refine_guard == 0.0 ? 1.5 : o.refine_guard;
     const bool guards = adaptive && gfac > 1.0;
     double guard_bar = -1.0;
     if (guards) {
@@ -506,6 +506,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
         // filter's noise far up the spectrum); the later ones from just above
         // the guarded set, so the out-of-set modes next to b are damped too
         rp.near_c = sw > 0 && nearf > 0.0 && !theta.empty() ? nearf * theta.back() : 0.0;
+        rp.low_x = theta.empty() ? 0.0 : theta.front();
         RefineStats rs;
         if ((rc = refine64(c, U, nc, theta, res->xintv[3], rp, &rs))) {
           cudaFree(U);

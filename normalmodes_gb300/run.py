@@ -217,46 +217,71 @@ class Group:
             self._own = False
 
 
-def _save_slice(path: str, r) -> None:
+def _num(v):
+    return float(v) if isinstance(v, float) else int(v)
+
+
+def _save_slice(path: str, r, key: str) -> None:
     """Checkpoint of one solved slice (written to a temporary name first, so
-    an interrupted write leaves no checkpoint)."""
+    an interrupted write leaves no checkpoint).  `key` names the slice, the
+    job and the solver settings it was solved with."""
     tmp = path + ".part.npz"
     vec = r.vec if r.vec is not None else np.zeros((0, 0))
     np.savez(tmp, lam=r.lam, err_ref=r.err_ref, res2=r.res2, vec=vec, xintv=np.asarray(r.xintv, dtype=np.float64),
              pol_deg=int(r.pol_deg), lanczos_steps=int(r.lanczos_steps),
              times=json.dumps({k: float(v) for k, v in r.times.items()}),
-             counts=json.dumps({k: int(v) for k, v in r.counts.items()}))
+             counts=json.dumps({k: _num(v) for k, v in r.counts.items()}), key=key)
     os.replace(tmp, path)
 
 
-def _load_slice(path: str):
+def _load_slice(path: str, key: str):
+    """The checkpoint at `path` if it was saved under the same `key` (slice,
+    job, solver settings), else None."""
     from types import SimpleNamespace
     with np.load(path) as z:
+        if "key" not in z.files or str(z["key"]) != key:
+            return None
         return SimpleNamespace(lam=z["lam"], err_ref=z["err_ref"], res2=z["res2"], vec=z["vec"],
                                xintv=tuple(z["xintv"]), pol_deg=int(z["pol_deg"]),
                                lanczos_steps=int(z["lanczos_steps"]), times=json.loads(str(z["times"])),
                                counts=json.loads(str(z["counts"])))
 
 
-def _solve(sv, job: Job, block: int, slices: int, out, grp: Group, ckpt: str | None = None, resume: bool = False):
+def _write_json(path: str, obj) -> None:
+    """JSON written to a temporary name and moved into place."""
+    tmp = path + ".part"
+    with open(tmp, "w") as f:
+        json.dump(obj, f)
+    os.replace(tmp, path)
+
+
+def _solve(sv, job: Job, block: int, slices: int, out, grp: Group, ckpt: str | None = None, resume: bool = False,
+           settings: str = ""):
     """One interval (nm_solve), or `slices` slices of equal estimated
     eigenvalue count (nm_slice_spectrum, on the first rank) solved on this
     rank's context (nm_solve_batched): slice j belongs to rank j mod size.
     With `ckpt` every solved slice (and the slice list) is saved under that
-    prefix; with `resume` saved slices are loaded instead of solved.
+    prefix, keyed by `settings` (job and solver settings) and the slice's
+    interval; with `resume` saved slices with the same key are loaded
+    instead of solved, and any other is solved again.
     Returns this rank's eigenpairs in ascending order and per-slice records."""
     if slices <= 1:
         cuts, counts = [(job.lowfreq, job.upfreq)], [None]
     else:
         saved = ckpt + "_slices.json" if ckpt else None
+        cc = None
         if grp.rank == 0 and resume and saved and os.path.exists(saved):
-            cc = json.load(open(saved))
-            cc = ([tuple(c) for c in cc["cuts"]], cc["counts"])
-        elif grp.rank == 0:
+            with open(saved) as f:
+                cs = json.load(f)
+            if cs.get("settings") == settings and cs.get("slices") == slices:
+                cc = ([tuple(c) for c in cs["cuts"]], cs["counts"])
+            else:
+                print(f" {saved} was saved for other settings: the slices are cut again", file=out)
+        if grp.rank == 0 and cc is None:
             cc = sv.slice_spectrum(job.lowfreq, job.upfreq, slices)
             cc = ([tuple(map(float, c)) for c in cc[0]], [float(x) for x in cc[1]])
             if saved:
-                json.dump({"cuts": cc[0], "counts": cc[1]}, open(saved, "w"))
+                _write_json(saved, {"settings": settings, "slices": slices, "cuts": cc[0], "counts": cc[1]})
         cuts, counts = grp.bcast(cc if grp.rank == 0 else None)
         print(" spectrum slices (mHz) and estimated eigenvalue counts:", file=out)
         for j, ((a, b), c) in enumerate(zip(cuts, counts)):
@@ -265,16 +290,20 @@ def _solve(sv, job: Job, block: int, slices: int, out, grp: Group, ckpt: str | N
     rs = []
     for j in mine:
         path = f"{ckpt}_slice{j}.npz" if ckpt else None
+        key = json.dumps({"settings": settings, "slice": [float(cuts[j][0]), float(cuts[j][1])]})
         if resume and path and os.path.exists(path):
-            rs.append(_load_slice(path))
-            print(f" slice {j}: resumed from {path}", file=out)
-            continue
+            r = _load_slice(path, key)
+            if r is not None:
+                rs.append(r)
+                print(f" slice {j}: resumed from {path}", file=out)
+                continue
+            print(f" slice {j}: {path} was saved for another slice or other settings: solved again", file=out)
         if len(cuts) == 1:
             r = sv.solve(job.lowfreq, job.upfreq, want_vectors=True, unscale=True, block=block)
         else:
             r = sv.solve_batched([cuts[j]], want_vectors=True, unscale=True, block=block)[0]
         if path:
-            _save_slice(path, r)
+            _save_slice(path, r, key)
         rs.append(r)
     if rs:
         lam = np.concatenate([r.lam for r in rs])
@@ -290,7 +319,7 @@ def _solve(sv, job: Job, block: int, slices: int, out, grp: Group, ckpt: str | N
              "estimated_count": None if counts[j] is None else float(counts[j]), "nev": int(len(r.lam)),
              "xintv": [float(x) for x in r.xintv], "filter_degree": int(r.pol_deg),
              "lanczos_steps": int(r.lanczos_steps), "times_s": {k: float(v) for k, v in r.times.items()},
-             "operator_counts": {k: int(v) for k, v in r.counts.items()}}
+             "operator_counts": {k: _num(v) for k, v in r.counts.items()}}
             for j, r in zip(mine, rs)]
     return lam[order], err[order], res2[order], vec[:, order] if vec.size else vec, meta
 
@@ -367,7 +396,10 @@ def _run(job, mixed, block, dry_run, out, say, slices, grp, lead, checkpoint, re
     with make_solver(model.operators(), job.porder, mixed, device=grp.local) as sv:
         log.stamp()
         log.phase("solve the eigenvalue problem")
-        lam, err, res2, vec, meta = _solve(sv, job, block, slices, say, grp, ckpt, resume)
+        settings = json.dumps({"base": job.base_path, "pOrder": job.porder, "JOB": job.job,
+                               "lowfreq": job.lowfreq, "upfreq": job.upfreq, "precision": "mixed" if mixed else "fp64",
+                               "block": block, "n": info.n, "np": info.np, "ntet": info.ntet})
+        lam, err, res2, vec, meta = _solve(sv, job, block, slices, say, grp, ckpt, resume, settings)
         log.stamp()
     # global ascending order: the first rank ranks every eigenvalue, each
     # rank learns the file indices of its own

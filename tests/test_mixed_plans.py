@@ -87,12 +87,12 @@ def test_refinement_plan_narrow_spectrum_and_off():
     assert _plan([1e-3, 0.4, 0.0, 1.0], 0)[1] is False
 
 
-def _refine_band(theta, res2, lmax, tol, near_c):
+def _refine_band(theta, res2, lmax, tol, near_c, low_x=0.0):
     t = np.ascontiguousarray(theta, dtype=np.float64)
     r = np.ascontiguousarray(res2, dtype=np.float64)
-    out = np.zeros(3)
-    nmgpu.lib().nm_test_refine_band(_dp(t), _dp(r), len(t), lmax, tol, near_c, _dp(out))
-    return out[0], int(out[1]), out[2]
+    out = np.zeros(4)
+    nmgpu.lib().nm_test_refine_band(_dp(t), _dp(r), len(t), lmax, tol, near_c, low_x, _dp(out))
+    return out[0], int(out[1]), out[2], out[3]
 
 
 def _degree(theta, res2, c, lmax, tol):
@@ -108,6 +108,12 @@ def _growth(theta, c, lmax, d):
     return max(d * (a0 - math.acosh(1 + 2 * (c - t) / (lmax - c))) for t in theta)
 
 
+def _low_growth(theta, c, lmax, d, low_x):
+    a = lambda x: math.acosh(1 + 2 * (c - x) / (lmax - c))
+    xs = [low_x * 10 ** (-0.25 * k) for k in range(33)]
+    return max(math.log(x / t) + d * (a(x) - a(t)) for t in theta if t > low_x for x in xs)
+
+
 # a block of 32 Ritz values of a 1.2M-DOF-like spectrum (lmax / b ~ 1e3)
 _TH = np.linspace(1.0e-4, 1.5e-4, 32)
 _LMAX = 0.2
@@ -120,32 +126,39 @@ def test_refinement_first_pass_band(res2):
     acosh(4 (lmax / theta) res2 / tol) / acosh(1 + 2 (c - theta) / (lmax - c))."""
     r = np.full(32, res2)
     tol = 1e-10 * math.sqrt(1.2e6)
-    c, d, g = _refine_band(_TH, r, _LMAX, tol, 0.0)
+    c, d, g, _ = _refine_band(_TH, r, _LMAX, tol, 0.0)
     assert c == pytest.approx(8 * _TH.max(), rel=1e-15)
     assert d == _degree(_TH, r, c, _LMAX, tol)
     if d:
         assert g == pytest.approx(_growth(_TH, c, _LMAX, d), rel=1e-12)
 
 
-@pytest.mark.parametrize("res2,near", [(1e-6, 1.05 * 1.3 * 1.5e-4), (1e-3, 1.05 * 1.3 * 1.5e-4), (1e-7, 1.6e-4)])
-def test_refinement_near_pass_band_bounds_growth(res2, near):
+@pytest.mark.parametrize("res2,near,low_x", [(1e-6, 1.05 * 1.5 * 1.5e-4, 0.0), (1e-3, 1.05 * 1.5 * 1.5e-4, 0.0),
+                                            (1e-7, 1.6e-4, 0.0), (1e-6, 1.05 * 1.5 * 1.5e-4, 4e-6),
+                                            (1e-6, 1.05 * 1.5 * 1.5e-4, 6e-5)])
+def test_refinement_near_pass_band_bounds_growth(res2, near, low_x):
     """Later passes: the band starts at near_c (or 1.05 x the block's top),
     moved up only as far as needed to keep the growth below the Ritz
-    values, d (acosh l(0) - acosh l(theta)), under log 1e3."""
+    values, d (acosh l(0) - acosh l(theta)), under log 1e3, and the gain of
+    the modes in (0, low_x] below the refined set, log(x / theta) +
+    d (acosh l(x) - acosh l(theta)), under log 2."""
     r = np.full(32, res2)
     tol = 1e-10 * math.sqrt(1.2e6)
-    c, d, g = _refine_band(_TH, r, _LMAX, tol, near)
+    c, d, g, gl = _refine_band(_TH, r, _LMAX, tol, near, low_x)
     lo = max(near, 1.05 * _TH.max())
     assert lo <= c <= 8 * _TH.max()
     assert d == _degree(_TH, r, c, _LMAX, tol)
     assert g == pytest.approx(_growth(_TH, c, _LMAX, d), rel=1e-12)
-    lim = math.log(1e3)
+    lim, lim_low = math.log(1e3), math.log(2.0)
+    if low_x > 0:
+        assert gl == pytest.approx(_low_growth(_TH, c, _LMAX, d, low_x), rel=1e-12, abs=1e-12)
+        assert gl <= lim_low + 1e-9
+    assert g <= lim + 1e-9
     if c > lo * (1 + 1e-12):
-        assert g <= lim + 1e-9
         c2 = c * (1 - 1e-6)
-        assert _growth(_TH, c2, _LMAX, _degree(_TH, r, c2, _LMAX, tol)) > lim - 1e-3
-    else:
-        assert g <= lim + 1e-9
+        d2 = _degree(_TH, r, c2, _LMAX, tol)
+        assert (_growth(_TH, c2, _LMAX, d2) > lim - 1e-3 or
+                (low_x > 0 and _low_growth(_TH, c2, _LMAX, d2, low_x) > lim_low - 1e-3))
 
 
 def test_filter_value_matches_chebyshev_series():

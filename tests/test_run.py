@@ -5,6 +5,7 @@ reference gravity, and whole jobs, single-interval and sliced, whose GPU
 context is replaced by the oracle (the printed tables and the result
 files)."""
 import io
+import json
 import os
 
 import numpy as np
@@ -257,4 +258,34 @@ def test_checkpoint_and_resume(tmp_path, monkeypatch):
     assert len(solved) == 1
     assert out.getvalue().count("resumed from") == 2
     assert again["nev"] == first["nev"]
+    assert np.array_equal(again["lam"], first["lam"])
+
+
+def test_resume_refuses_checkpoints_of_other_settings(tmp_path, monkeypatch):
+    """A checkpoint saved with other solver settings (here FP64 against a
+    mixed-precision resume) is not merged: the slices are cut again and
+    every slice is solved again, with the same result."""
+    conf = _job_files(tmp_path, 2)
+    monkeypatch.setattr(R, "make_solver", _OracleSolver)
+    first = R.run(R.read_global_conf(conf), out=io.StringIO(), slices=3, checkpoint=True)
+    ck = first["prefix"] + "_ckpt"
+    with open(ck + "_slices.json") as f:
+        assert json.load(f)["slices"] == 3
+    solved, cut = [], []
+
+    class Counting(_OracleSolver):
+        def slice_spectrum(self, lo, hi, n):
+            cut.append(n)
+            return super().slice_spectrum(lo, hi, n)
+
+        def solve_batched(self, cuts, want_vectors, unscale, block):
+            solved.extend(cuts)
+            return super().solve_batched(cuts, want_vectors, unscale, block)
+
+    monkeypatch.setattr(R, "make_solver", Counting)
+    out = io.StringIO()
+    again = R.run(R.read_global_conf(conf), mixed=True, block=0, out=out, slices=3, resume=True)
+    assert cut == [3] and len(solved) == 3
+    assert "cut again" in out.getvalue() and out.getvalue().count("solved again") == 3
+    assert "resumed from" not in out.getvalue()
     assert np.array_equal(again["lam"], first["lam"])
