@@ -43,6 +43,8 @@ def main(argv=None) -> None:
     ap.add_argument("--refine-near", type=float, default=0.0,
                     help="later passes: band from this x the top guarded Ritz value (0: 1.05; < 0: band passes)")
     ap.add_argument("--skip-fp64", action="store_true", help="mixed path only (no comparison)")
+    ap.add_argument("--mixed-lam", default=None,
+                    help="eigenvalues of an earlier mixed solve (.npy): run the FP64 solve only and compare")
     ap.add_argument("--orth", type=int, default=0,
                     help="mixed Gram-Schmidt: 0 tensor-core projection, 1 FP64, 2 cuBLAS SGEMM")
     ap.add_argument("--verbose", action="store_true")
@@ -60,8 +62,8 @@ def main(argv=None) -> None:
            "refine_guard": a.refine_guard, "refine_near": a.refine_near,
            "refine_growth": a.refine_growth}
     res = {}
-    runs = [("mixed", NM_PREC_MIXED, 32)] + ([] if (a.fp64_lam or a.skip_fp64) else
-                                              [("fp64", NM_PREC_FP64, a.fp64_block)])
+    runs = ([] if a.mixed_lam else [("mixed", NM_PREC_MIXED, 32)]) + \
+        ([] if (a.fp64_lam or a.skip_fp64) else [("fp64", NM_PREC_FP64, a.fp64_block)])
     for name, prec, block in runs:
         with Solver(mats, a.porder, precision=prec, inner_tol=a.inner_tol, verbose=a.verbose, orth=a.orth) as sv:
             t = time.perf_counter()
@@ -82,22 +84,22 @@ def main(argv=None) -> None:
                      "refinement": {k: r.counts[k] for k in ("refine_passes", "refine_blocks", "refine_maxdeg",
                                                              "refine_steps", "res2_before_refine",
                                                              "refine_guards")}}
-    m = res["mixed"].lam
+    m = np.load(a.mixed_lam) if a.mixed_lam else res["mixed"].lam
+    if a.save_mixed_lam and "mixed" in res:
+        np.save(a.save_mixed_lam, res["mixed"].lam)
     if a.skip_fp64 and not a.fp64_lam:
         print(json.dumps(out))
         return
     f = np.load(a.fp64_lam) if a.fp64_lam else res["fp64"].lam
     if a.save_fp64_lam and "fp64" in res:
         np.save(a.save_fp64_lam, f)
-    if a.save_mixed_lam:
-        np.save(a.save_mixed_lam, res["mixed"].lam)
     out["same_count"] = len(m) == len(f)
     if len(m) == len(f) and len(f):
         rel = np.abs(m - f) / np.abs(f)
         out["eig_rel_diff_max"] = float(rel.max())
         out["eig_rel_diff_median"] = float(np.median(rel))
         out["eig_rel_diff"] = [float(x) for x in rel]
-    if "fp64" in out:
+    if "fp64" in out and "mixed" in out:
         out["speedup_mixed_over_fp64"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
     print(json.dumps(out))
 
