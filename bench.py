@@ -71,8 +71,9 @@ WORKLOADS = {
 # Step counts of the reference algorithm (single-vector ChebLanNr, FP64) on
 # the 1.2M-DOF ball, used only to project the CPU samples: the filter degree
 # (125) and eigenpair count (1232) are those of the GPU solves of this
-# workload; the Lanczos steps are the block path's 4992 vectors on this
-# ball times the single-vector / block ratio measured on the 24^3 ball at
+# workload, FP64 and mixed alike; the Lanczos steps are the 4992 block
+# vectors that both the FP64 and the mixed block paths take on this ball,
+# times the single-vector / block ratio measured on the 24^3 ball at
 # 0.1-1.0 mHz (801 single-vector steps against 1152 block vectors for the
 # same 203 eigenpairs, both on one GB300): 4992 * 801 / 1152 = 3471.
 REF_COUNTS = {"ball36-p2-lateral": dict(nev=1232, lanczos_steps=3471, degree=125),
