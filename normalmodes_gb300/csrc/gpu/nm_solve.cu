@@ -517,8 +517,9 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
         res->refine_maxdeg = std::max(res->refine_maxdeg, rs.max_deg);
         if (sw == 0) res->res2_before_refine = rs.max_res2_before;
         if (c->verbose)
-          printf(" refinement pass %d: %d blocks, %lld block degree steps (max degree %d), res2 before %.3e\n",
-                 sw + 1, rs.blocks, rs.steps, rs.max_deg, rs.max_res2_before);
+          printf(" refinement pass %d: %d blocks, %lld block degree steps (max degree %d), res2 before %.3e "
+                 "(wanted %.3e, %d above the target)\n",
+                 sw + 1, rs.blocks, rs.steps, rs.max_deg, rs.max_res2_before, rs.max_res2_want, rs.want_above);
         if (rs.blocks == 0) break;
         if ((rc = rayleigh_ritz64(c, &U, nc, &theta))) {
           cudaFree(U);
