@@ -470,9 +470,11 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
         return rc;
       }
       progress(c, NM_PHASE_RITZ, nc, nc);
-      if (refine && guards) {
-        // keep the Ritz vectors with quotients in [a / g, g b] (ascending
-        // after the Rayleigh-Ritz); the rest of the filter's tail goes
+      // keep the Ritz vectors with quotients in [a / g, g b] (ascending
+      // after each Rayleigh-Ritz): the filter's tail goes after the first,
+      // and a column whose quotient left the window (a mixture drifting to
+      // the null space or far up) after any later one
+      auto keep_window = [&]() -> int {
         int i0 = 0, i1 = nc;
         while (i0 < nc && theta[i0] < xintv[0] / gfac) ++i0;
         while (i1 > i0 && theta[i1 - 1] > gfac * xintv[1]) --i1;
@@ -482,6 +484,13 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
                                        cudaMemcpyDeviceToDevice, c->stream));
         theta = std::vector<double>(theta.begin() + i0, theta.begin() + i1);
         nc = i1 - i0;
+        return NM_OK;
+      };
+      if (refine && guards) {
+        if ((rc = keep_window())) {
+          cudaFree(U);
+          return rc;
+        }
         res->refine_guards = 0;
         for (double t : theta) res->refine_guards += t < xintv[0] || t > xintv[1];
       }
@@ -526,6 +535,10 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
           return rc;
         }
         ++res->refine_passes;
+        if (guards && (rc = keep_window())) {
+          cudaFree(U);
+          return rc;
+        }
         // residuals measured before this pass against those before the last
         if (o.refine_sweeps <= 0 && sw >= 2 && !(rs.max_res2_want < 0.5 * prev_want)) break;
         prev_want = rs.max_res2_want;
