@@ -200,6 +200,12 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
                   double* t_filter, double* t_orth, double* t_eig, double guard_bar = -1.0, int max_guard = -1);
 // Value of the filter polynomial p at x (the Chebyshev series of pol).
 double filter_value(const Pol& pol, double x);
+// Index of the first Ritz value kept from the K ascending filter values
+// evals: those >= bar, and when 0 < guard_bar < bar up to max_guard (-1:
+// half the count above the bar plus 64) more in [guard_bar, bar).
+int ritz_first(const double* evals, int K, double bar, double guard_bar, int max_guard);
+// [i0, i1): the ascending theta[0..n) within [lo, hi].
+void window_range(const double* theta, int n, double lo, double hi, int* i0, int* i1);
 // FP64 Rayleigh-Ritz on the columns of U (n x nc): U <- U Q with
 // (U^T A U) Q = (U^T B U) Q Theta.  Resolves the mixing of close Ritz pairs
 // left by an FP32 filter.

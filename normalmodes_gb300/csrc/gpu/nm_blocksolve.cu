@@ -266,6 +266,31 @@ int cheb_degree_for(const ChebSetup& ref, double eps) {
   return std::max(1, std::min(ref.deg, d));
 }
 
+int ritz_first(const double* evals, int K, double bar, double guard_bar, int max_guard) {
+  int first = K;
+  for (int i = 0; i < K; ++i)
+    if (evals[i] >= bar) {
+      first = i;
+      break;
+    }
+  if (guard_bar > 0.0 && guard_bar < bar && first < K) {
+    // guards: the next Ritz values below the bar, largest filter value first
+    const int cap = max_guard >= 0 ? max_guard : (K - first) / 2 + 64;
+    int g0 = first;
+    while (g0 > 0 && first - g0 < cap && evals[g0 - 1] >= guard_bar) --g0;
+    first = g0;
+  }
+  return first;
+}
+
+void window_range(const double* theta, int n, double lo, double hi, int* i0, int* i1) {
+  int a = 0, b = n;
+  while (a < n && theta[a] < lo) ++a;
+  while (b > a && theta[b - 1] > hi) --b;
+  *i0 = a;
+  *i1 = b;
+}
+
 // p(x) of a filter polynomial: sum_k mu_k T_k((x - cc) / dd).
 double filter_value(const Pol& pol, double x) {
   const double l0 = (x - pol.cc) / pol.dd;
@@ -978,19 +1003,7 @@ int block_lanczos(nm_ctx* c, const Pol& pol, int maxit, bool use_graph, double**
   // ---- Ritz vectors for eigenvalues of T above the bar
   const int K = nblk * S;
   if ((rc = eig_T(nblk, true))) return fail(rc);
-  int first = K;
-  for (int i = 0; i < K; ++i)
-    if (evals[i] >= pol.bar) {
-      first = i;
-      break;
-    }
-  if (guard_bar > 0.0 && guard_bar < pol.bar && first < K) {
-    // guards: the next Ritz values below the bar, largest filter value first
-    const int cap = max_guard >= 0 ? max_guard : (K - first) / 2 + 64;
-    int g0 = first;
-    while (g0 > 0 && first - g0 < cap && evals[g0 - 1] >= guard_bar) --g0;
-    first = g0;
-  }
+  const int first = ritz_first(evals.data(), K, pol.bar, guard_bar, max_guard);
   const int nc = K - first;
   double* U = nullptr;
   if (nc > 0) {
@@ -1654,6 +1667,14 @@ int nm_test_cheb_degree(double lmin, double lmax, int ref_deg, double eps) {
 double nm_test_filter_at_zero(const double* xintv, double thresh_int, double thresh_ext, int damping) {
   const nmg::Pol P = nmg::find_pol(xintv, thresh_int, thresh_ext, 2, 10000, damping);
   return nmg::filter_at_zero(P);
+}
+// Ritz selection of the block Lanczos: index of the first kept eigenvalue of
+// T (ascending filter values) and the guard window of the refinement
+int nm_test_ritz_first(const double* evals, int K, double bar, double guard_bar, int max_guard) {
+  return nmg::ritz_first(evals, K, bar, guard_bar, max_guard);
+}
+void nm_test_window_range(const double* theta, int n, double lo, double hi, int* out) {
+  nmg::window_range(theta, n, lo, hi, out, out + 1);
 }
 // adaptive refinement of one block (purge form): out = {band start c0,
 // degree, log growth, log low growth}; near_c <= 0 for a first (band 8) pass

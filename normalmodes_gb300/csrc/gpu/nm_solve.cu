@@ -476,8 +476,7 @@ int nm_solve(nm_ctx* c, double f_lo, double f_hi, const nm_solve_opts* opts, nm_
       // the null space or far up) after any later one
       auto keep_window = [&]() -> int {
         int i0 = 0, i1 = nc;
-        while (i0 < nc && theta[i0] < xintv[0] / gfac) ++i0;
-        while (i1 > i0 && theta[i1 - 1] > gfac * xintv[1]) --i1;
+        window_range(theta.data(), nc, xintv[0] / gfac, gfac * xintv[1], &i0, &i1);
         if (i0 > 0)
           for (int j = i0; j < i1; ++j)
             NM_CUDA(c, cudaMemcpyAsync(U + (size_t)(j - i0) * n, U + (size_t)j * n, sizeof(double) * n,

@@ -229,6 +229,9 @@ def lib() -> C.CDLL:
         L.nm_test_filter_at_zero.restype = C.c_double
         L.nm_test_polish_plan.argtypes = [dp, C.c_int, C.POINTER(C.c_int), dp]
         L.nm_test_refine_band.argtypes = [dp, dp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, dp]
+        L.nm_test_ritz_first.argtypes = [dp, C.c_int, C.c_double, C.c_double, C.c_int]
+        L.nm_test_ritz_first.restype = C.c_int
+        L.nm_test_window_range.argtypes = [dp, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int)]
         L.nm_test_filter_value.argtypes = [dp, C.c_double, C.c_double, C.c_int, C.c_double]
         L.nm_test_filter_value.restype = C.c_double
         L.nm_test_polish_block.argtypes = [dp, C.c_int, C.c_double, C.c_double, dp]

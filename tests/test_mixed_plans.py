@@ -169,3 +169,36 @@ def test_filter_value_matches_chebyshev_series():
         ref = np.polynomial.chebyshev.chebval((lam - p.cc) / p.dd, p.mu)
         got = nmgpu.lib().nm_test_filter_value(_dp(x), 0.8, 0.7, 1, lam)
         assert abs(got - ref) <= 1e-12 * max(1.0, abs(ref))
+
+
+def _ritz_first(evals, bar, guard_bar, max_guard=-1):
+    e = np.ascontiguousarray(evals, dtype=np.float64)
+    return nmgpu.lib().nm_test_ritz_first(_dp(e), len(e), bar, guard_bar, max_guard)
+
+
+def test_ritz_selection_with_guards():
+    """The block Lanczos keeps the Ritz values of T (ascending filter
+    values) at or above the bar, and with a guard bar up to a cap more just
+    below it, largest filter value first."""
+    ev = np.array([0.0, 0.01, 0.05, 0.2, 0.5, 0.79, 0.8, 0.9, 1.0])
+    assert _ritz_first(ev, 0.8, -1.0) == 6                 # no guards: the bar alone
+    assert _ritz_first(ev, 0.8, 0.9) == 6                  # a guard bar above the bar is ignored
+    assert _ritz_first(ev, 0.8, 0.1) == 3                  # 0.79, 0.5, 0.2 join as guards
+    assert _ritz_first(ev, 0.8, 0.1, max_guard=2) == 4     # capped at two
+    assert _ritz_first(ev, 0.8, 1e-9) == 1                 # default cap (3 / 2 + 64) does not bind
+    assert _ritz_first(ev, 1.1, 0.1) == len(ev)            # nothing above the bar: no guards either
+    big = np.linspace(0.0, 1.0, 1000)
+    first = _ritz_first(big, 0.9, 1e-9)
+    above = int(np.sum(big >= 0.9))
+    assert len(big) - first == above + above // 2 + 64     # default cap
+
+
+def test_guard_window():
+    """The refinement keeps the ascending Rayleigh quotients within
+    [a / g, g b]."""
+    th = np.ascontiguousarray([1e-9, 0.5, 0.7, 1.0, 2.0, 2.9, 3.1, 10.0])
+    out = (C.c_int * 2)()
+    nmgpu.lib().nm_test_window_range(_dp(th), len(th), 1.0 / 1.5, 2.0 * 1.5, out)
+    assert (out[0], out[1]) == (2, 6)
+    nmgpu.lib().nm_test_window_range(_dp(th), len(th), 20.0, 30.0, out)
+    assert out[0] == out[1]
